@@ -1,0 +1,213 @@
+/*
+ * kcore.h -- C ABI of the pico_gb300 k-core engine (libkcore.so).
+ *
+ * GB300-native replacement for the k-core path of chriszhao13/pico.  The
+ * reference has no library interface: each method is a CUDA executable whose
+ * main() loads a MatrixMarket file, builds a graph on the host, iterates its
+ * kernels from a host loop and prints a report.  This header exposes that
+ * path as plain C entry points (pointers and sizes only) so any host language
+ * can bind it; each declaration names the reference code it replaces.
+ *
+ * Conventions
+ *   - Every call returns an int status: KC_OK (0) or a KC_ERR_* code.  Nothing
+ *     here exits the process or traps the GPU; kc_last_error() returns a
+ *     message for the calling thread's last failure.
+ *   - A kc_graph owns a device-resident CSR (int64 row offsets, uint32 column
+ *     ids, both directions of every edge, no self-loops) plus the work buffers
+ *     of the decomposition.  One graph is used by one host thread at a time;
+ *     different graphs are independent.
+ *   - `stream` arguments are cudaStream_t values passed as void*; NULL selects
+ *     the graph's own stream.
+ *   - Core numbers are uint32, one per vertex in [0, n).
+ */
+#ifndef PICO_GB300_KCORE_H
+#define PICO_GB300_KCORE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define KC_ABI_VERSION 1
+
+/* Status codes. */
+enum {
+    KC_OK = 0,
+    KC_ERR_INVALID = 1,     /* bad argument, id out of range, malformed input line */
+    KC_ERR_IO = 2,          /* file cannot be opened or read */
+    KC_ERR_CUDA = 3,        /* CUDA runtime error (message in kc_last_error) */
+    KC_ERR_NOMEM = 4,       /* device or host allocation failed / not admitted */
+    KC_ERR_CAPACITY = 5,    /* a bounded device queue or table overflowed */
+    KC_ERR_TIMEOUT = 6,     /* a device-side wait exceeded its limit; results invalid */
+    KC_ERR_UNSUPPORTED = 7, /* feature not available (e.g. no cooperative launch) */
+    KC_ERR_STATE = 8        /* call not valid in the object's current state */
+};
+
+/* Decomposition methods: the seven reference drivers plus automatic choice.
+ * All produce the exact core numbers; KC_GPP additionally reports core 1 for
+ * degree-0 vertices, as peel/gppeel.cu:247-252 does. */
+enum {
+    KC_HISTO = 0,       /* index2core/HistoCore.cu   h-index iteration        */
+    KC_CNT = 1,         /* index2core/CntCore.cu     h-index iteration        */
+    KC_NBR = 2,         /* index2core/NbrCore.cu     h-index iteration        */
+    KC_PEELONE = 3,     /* peel/peelone.cu           bucket peel              */
+    KC_GPP = 4,         /* peel/gppeel.cu            bucket peel (+ deg0 -> 1) */
+    KC_PEELONE_DYN = 5, /* peel/src/peelone-dyn.cc   bucket peel              */
+    KC_PEEL_DYN = 6,    /* peel/src/peel-dyn.cc      bucket peel              */
+    KC_AUTO = 7         /* engine's choice (autotuned)                        */
+};
+
+/* MatrixMarket loader semantics. */
+enum {
+    /* Graph::ReadGraph + VirtualGraph (index2core/shared/graph.cpp:17-95,
+     * virtual_graph.cpp:16-44): skip 2 lines, keep duplicate lines as parallel
+     * edges, drop self-loops; n = max id (+1 if id 0 occurs); ids shifted to
+     * 0-based when id 0 does not occur. */
+    KC_LOAD_COO = 0,
+    /* Graph::readFile (peel/src/graph.cpp:58-133): 1-based ids, self-loops
+     * dropped, neighbours de-duplicated and sorted, V = max id. */
+    KC_LOAD_CSR_DEDUP = 1
+};
+
+/* Flags for kc_graph_from_edges*. */
+#define KC_EDGES_DEDUP 1u      /* remove parallel edges, sort each row */
+#define KC_EDGES_SORT_ROWS 2u  /* sort each row by neighbour id (keeps parallel edges) */
+
+typedef struct kc_graph kc_graph;
+
+typedef struct kc_stats {
+    uint32_t method;      /* method actually run */
+    uint32_t iterations;  /* peel: levels processed; h-index: sweeps */
+    uint32_t levels;      /* peel: distinct non-empty levels (= distinct core values) */
+    uint32_t kmax;        /* largest core number ("Max K") */
+    uint32_t kmin;        /* reference's "Min K": min(10, smallest core) (util.cpp:6-22) */
+    uint32_t reserved;
+    uint64_t n;           /* vertices */
+    uint64_t nnz;         /* directed CSR entries (2 x undirected edges) */
+    double ms;            /* device time of the decomposition (CUDA events) */
+    double build_ms;      /* device time of the CSR build that made this graph */
+} kc_stats;
+
+/* ---- library ---------------------------------------------------------- */
+int kc_abi_version(void);
+/* Message describing the calling thread's most recent failure ("" if none). */
+const char *kc_last_error(void);
+/* Number of CUDA devices visible (0 without a GPU; never fails). */
+int kc_device_count(void);
+
+/* ---- graph construction ----------------------------------------------- */
+/* Load a MatrixMarket file (mode = KC_LOAD_*) and build it on `device`.
+ * Replaces Graph::ReadGraph + VirtualGraph::MakeUGraph + the cudaMemcpy block
+ * of each index2core/peel main() (e.g. HistoCore.cu:207-286), and the
+ * Graph(std::string) + malloc_graph_gpu_memory of peel/main.cu:65 /
+ * peel/src/gpu_memory_allocation.cu:4-12. */
+int kc_graph_from_mtx(const char *path, int mode, int device, kc_graph **out);
+
+/* Parse a MatrixMarket file on the host only (no GPU needed).  On success
+ * *src / *dst hold *m 0-based endpoints (self-loops already dropped) in file
+ * order, and *n the vertex count, with `mode` semantics.  Free with
+ * kc_host_free_edges.  Restates the two loaders above for host callers. */
+int kc_parse_mtx(const char *path, int mode, uint32_t *n, uint64_t *m, uint32_t **src, uint32_t **dst);
+void kc_host_free_edges(uint32_t *src, uint32_t *dst);
+
+/* Build from an undirected edge list in HOST memory: endpoints are 0-based
+ * and < n; self-loops are dropped; both directions are stored.  flags:
+ * KC_EDGES_DEDUP / KC_EDGES_SORT_ROWS; without either, each row keeps the
+ * edge-list order (the order MakeUGraph produces, virtual_graph.cpp:142-163).
+ * The device build: degree count, exclusive scan to int64 offsets, scatter,
+ * segmented row sort and unique. */
+int kc_graph_from_edges(const uint32_t *src, const uint32_t *dst, uint64_t m, uint32_t n,
+                        uint32_t flags, int device, kc_graph **out);
+/* Same with endpoints already in device memory of `device`. */
+int kc_graph_from_edges_device(const uint32_t *d_src, const uint32_t *d_dst, uint64_t m, uint32_t n,
+                               uint32_t flags, int device, kc_graph **out);
+
+/* Build from a CSR in HOST memory (rowptr[n+1] int64, col[rowptr[n]]).  The
+ * CSR must be symmetric without self-loops (not checked; see
+ * kc_graph_validate). */
+int kc_graph_from_csr(const int64_t *rowptr, const uint32_t *col, uint32_t n, int device, kc_graph **out);
+/* Same from device memory; the graph copies the arrays. */
+int kc_graph_from_csr_device(const int64_t *d_rowptr, const uint32_t *d_col, uint32_t n, int device,
+                             kc_graph **out);
+
+/* Check symmetry / self-loops / id range on the device.  *bad = number of
+ * offending entries (0 for a valid graph). */
+int kc_graph_validate(kc_graph *g, uint64_t *bad);
+
+int kc_graph_free(kc_graph *g);
+
+/* Sizes: n, directed entries, max degree, number of 32-wide virtual nodes. */
+int kc_graph_info(const kc_graph *g, uint32_t *n, uint64_t *nnz, uint32_t *max_degree,
+                  uint64_t *num_vnodes);
+/* Device pointers of the resident CSR (valid until kc_graph_free). */
+int kc_graph_device_csr(const kc_graph *g, const int64_t **d_rowptr, const uint32_t **d_col);
+/* Copy the CSR to host buffers (rowptr[n+1], col[nnz]). */
+int kc_graph_copy_csr(const kc_graph *g, int64_t *rowptr, uint32_t *col);
+/* Degrees (host buffer, n entries). */
+int kc_graph_degrees(const kc_graph *g, uint32_t *deg);
+
+/* Export the reference's virtual-graph layout built on the device
+ * (VirtualGraph::MakeUGraph, virtual_graph.cpp:96-192): nodePointer[n]
+ * (uint32 slot of deg(v)), edgeList[nnz+n] (deg(v) then the row), and
+ * parts[2*numParts] = {node, part} with ceil(deg/part_size) parts per vertex.
+ * Host output buffers; *num_parts receives numParts.  Pass parts == NULL to
+ * query *num_parts only.  Offsets must fit uint32 as in the reference. */
+int kc_graph_virtual_layout(kc_graph *g, uint32_t part_size, uint32_t *node_pointer,
+                            uint32_t *edge_list, uint32_t *parts, uint64_t *num_parts);
+
+/* ---- decomposition ----------------------------------------------------- */
+/* Core number of every vertex.  Replaces the timed loops of HistoCore.cu:292-341,
+ * CntCore.cu:344-417, NbrCore.cu:244-297, peelone.cu:157-186,
+ * gppeel.cu:398-440, int peelone_dyn(Graph&) (peelone-dyn.cc:120-168) and
+ * int peel_dyn(Graph&) (peel-dyn.cc:301-350).  core_out: n uint32 in host
+ * memory (out_on_device = 0) or device memory of the graph's device
+ * (out_on_device = 1); may be NULL to keep the result on the device only
+ * (see kc_graph_device_core).  stats may be NULL. */
+int kc_decompose(kc_graph *g, int method, uint32_t *core_out, int out_on_device, kc_stats *stats,
+                 void *stream);
+/* CUDA-event timings of the last decomposition on this graph: *total_ms
+ * covers every kernel of the call (initialisation included), *kernel_ms the
+ * main decomposition kernel alone.  Either pointer may be NULL. */
+int kc_graph_last_timing(const kc_graph *g, double *total_ms, double *kernel_ms);
+/* Device pointer of the last decomposition's core array (n uint32). */
+int kc_graph_device_core(const kc_graph *g, const uint32_t **d_core);
+
+/* ---- memory helpers ----------------------------------------------------
+ * The reference allocates and copies inside each driver
+ * (peel/src/gpu_memory_allocation.cu:4-21, HistoCore.cu:259-286); callers of
+ * this library use these to stage inputs and outputs. */
+/* Pinned host memory (fast host<->device copies). */
+int kc_host_alloc(void **p, size_t bytes);
+int kc_host_free(void *p);
+/* Device memory on `device`. */
+int kc_device_alloc(void **p, size_t bytes, int device);
+int kc_device_free(void *p);
+/* cudaMemcpy; kind: 1 = host->device, 2 = device->host, 3 = device->device. */
+int kc_memcpy(void *dst, const void *src, size_t bytes, int kind);
+/* Wait for all work on `device` to finish. */
+int kc_device_synchronize(int device);
+
+/* ---- seeded graph generators (device) ---------------------------------- */
+/* Generators write an undirected edge list (src, dst; 0-based) to DEVICE
+ * buffers of capacity `cap` edges and report the count in *m.  Counter-based
+ * hashing (splitmix64 finaliser) makes the output independent of the launch
+ * shape, so a host restatement reproduces it bit for bit. */
+/* R-MAT: 2^scale ids, edge_factor*2^scale draws, quadrant probabilities a,b,c
+ * (d = 1-a-b-c).  Self-loops and duplicates are kept (the builder drops them). */
+int kc_gen_rmat(uint32_t scale, uint64_t num_edges, double a, double b, double c, uint64_t seed,
+                uint32_t *d_src, uint32_t *d_dst, void *stream);
+/* Erdos-Renyi G(n, m): m distinct unordered pairs {u<v}, sampled without
+ * replacement through a keyed Feistel permutation of the pair index space. */
+int kc_gen_er(uint32_t n, uint64_t m, uint64_t seed, uint32_t *d_src, uint32_t *d_dst, void *stream);
+/* Planted dense subgraph: `k` distinct members of [0, n) chosen by a keyed
+ * permutation; each member pair is an edge with probability p.  Writes at
+ * most cap edges; *m receives the count (KC_ERR_CAPACITY if cap is short). */
+int kc_gen_planted(uint32_t n, uint32_t k, double p, uint64_t seed, uint32_t *d_src, uint32_t *d_dst,
+                   uint64_t cap, uint64_t *m, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PICO_GB300_KCORE_H */

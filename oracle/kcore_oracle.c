@@ -1,0 +1,368 @@
+/*
+ * kcore_oracle.c -- TEST INFRASTRUCTURE ONLY.
+ *
+ * CPU restatement of chriszhao13/pico's k-core algorithms, used as the parity
+ * checker for the CUDA engine in pico_gb300.  Only the tests, the smoke check
+ * and bench.py's CPU-baseline leg load this file; the product never does.
+ *
+ * Contents
+ *   orc_bz            serial Batagelj-Zaversnik bucket peel (Batagelj &
+ *                     Zaversnik, "An O(m) Algorithm for Cores Decomposition of
+ *                     Networks", 2003).  The reference has no CPU k-core code,
+ *                     so this is the primary oracle, written from the paper.
+ *   orc_hindex_jacobi synchronous h-index iteration restating the common
+ *                     trajectory of index2core/NbrCore.cu:78-113,244-297,
+ *                     index2core/CntCore.cu:82-130,344-417 and
+ *                     index2core/HistoCore.cu:77-128,292-341 (all three apply
+ *                     the h-index operator to every vertex whose neighbourhood
+ *                     changed, from core = degree).
+ *   orc_peel_rounds   level-synchronous peel restating peel/peelone.cu:14-91,
+ *                     157-186 with one round per kernel launch.
+ *   orc_gpp           two-phase scan/scatter peel restating
+ *                     peel/gppeel.cu:12-104,186-228, including its core = 1
+ *                     for degree-0 vertices.
+ *   orc_peel_dyn      per-level select + queue peel restating
+ *                     peel/src/peelone-dyn.cc:2-117,120-168.
+ *   orc_make_ugraph   inline-degree CSR + virtual nodes restating
+ *                     index2core/shared/virtual_graph.cpp:96-192.
+ *   orc_csr_dedup     sorted, de-duplicated CSR restating
+ *                     peel/src/graph.cpp:103-131.
+ *   orc_check_local   per-vertex fixpoint test of a core vector.
+ *
+ * Parity is pinned by the reference's own known answer (example.txt: every
+ * core is 2) and by golden files produced with the reference's own loader and
+ * virtual-graph code compiled from its sources (see oracle/build_ref.sh and
+ * tests/golden/make_golden.py).
+ *
+ * Graph input convention for the decomposition routines: CSR with int64 row
+ * offsets rowptr[n+1] and uint32 column ids col[rowptr[n]], both directions of
+ * every undirected edge present, no self-loops.  Parallel entries (the
+ * reference's COO loader keeps duplicate lines) count with multiplicity.
+ */
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define ORC_OK 0
+#define ORC_ENOMEM 4
+
+/* ------------------------------------------------------------------------ */
+/* Batagelj-Zaversnik (2003), Algorithm 1 of the paper: bin-sort vertices by
+ * degree, then repeatedly take the vertex of least residual degree and move
+ * each neighbour with a larger residual degree one bin down. O(n + m).      */
+int64_t orc_bz(uint32_t n, const int64_t *rowptr, const uint32_t *col, uint32_t *core)
+{
+    if (n == 0) return 0;
+    uint32_t md = 0;
+    for (uint32_t v = 0; v < n; v++) {
+        uint64_t d = (uint64_t)(rowptr[v + 1] - rowptr[v]);
+        core[v] = (uint32_t)d;
+        if (core[v] > md) md = core[v];
+    }
+    uint64_t *bin = (uint64_t *)calloc((size_t)md + 1, sizeof(uint64_t));
+    uint32_t *vert = (uint32_t *)malloc((size_t)n * sizeof(uint32_t));
+    uint32_t *pos = (uint32_t *)malloc((size_t)n * sizeof(uint32_t));
+    if (!bin || !vert || !pos) { free(bin); free(vert); free(pos); return -ORC_ENOMEM; }
+    for (uint32_t v = 0; v < n; v++) bin[core[v]]++;
+    uint64_t start = 0;
+    for (uint32_t d = 0; d <= md; d++) { uint64_t num = bin[d]; bin[d] = start; start += num; }
+    for (uint32_t v = 0; v < n; v++) { pos[v] = (uint32_t)bin[core[v]]; vert[pos[v]] = v; bin[core[v]]++; }
+    for (uint32_t d = md; d >= 1; d--) bin[d] = bin[d - 1];
+    bin[0] = 0;
+    uint32_t kmax = 0;
+    for (uint32_t i = 0; i < n; i++) {
+        uint32_t v = vert[i];
+        uint32_t cv = core[v];
+        if (cv > kmax) kmax = cv;
+        for (int64_t e = rowptr[v]; e < rowptr[v + 1]; e++) {
+            uint32_t u = col[e];
+            if (core[u] > cv) {
+                uint32_t du = core[u];
+                uint32_t pu = pos[u];
+                uint32_t pw = (uint32_t)bin[du];
+                uint32_t w = vert[pw];
+                if (u != w) { pos[u] = pw; vert[pu] = w; pos[w] = pu; vert[pw] = u; }
+                bin[du]++;
+                core[u]--;
+            }
+        }
+    }
+    free(bin); free(vert); free(pos);
+    return kmax;
+}
+
+/* ------------------------------------------------------------------------ */
+/* h-index of the multiset {min(cap, c[u]) : u in N(v)}: the largest k <= cap
+ * with at least k neighbours of value >= k.  `hist` has cap+1 zeroed slots and
+ * is left zeroed.  This is the suffix-sum scan of NbrCore.cu:97-104.        */
+static uint32_t hindex_of(const int64_t *rowptr, const uint32_t *col, const uint32_t *c,
+                          uint32_t v, uint32_t cap, uint32_t *hist)
+{
+    for (int64_t e = rowptr[v]; e < rowptr[v + 1]; e++) {
+        uint32_t x = c[col[e]];
+        hist[x < cap ? x : cap]++;
+    }
+    uint64_t sum = 0;
+    uint32_t k;
+    for (k = cap; k >= 1; k--) {
+        sum += hist[k];
+        if (sum >= k) break;
+    }
+    for (int64_t e = rowptr[v]; e < rowptr[v + 1]; e++) {
+        uint32_t x = c[col[e]];
+        hist[x < cap ? x : cap] = 0;
+    }
+    hist[0] = 0;
+    return k;
+}
+
+/* Synchronous (Jacobi) h-index iteration from core = degree.  Each sweep
+ * recomputes every vertex flagged by a neighbour's change in the previous
+ * sweep (all vertices in the first), reading the previous sweep's values, as
+ * the separate histogram / count / notify launches of NbrCore.cu:253-296 do.
+ * *iters receives the number of sweeps including the final sweep that changes
+ * nothing, i.e. the reference's "Number of iterations".                    */
+int orc_hindex_jacobi(uint32_t n, const int64_t *rowptr, const uint32_t *col, uint32_t *core,
+                      uint32_t *iters)
+{
+    uint32_t md = 0;
+    uint32_t *prev = (uint32_t *)malloc((size_t)n * sizeof(uint32_t) + 4);
+    uint8_t *flag = (uint8_t *)malloc((size_t)n + 1);
+    uint8_t *next = (uint8_t *)malloc((size_t)n + 1);
+    for (uint32_t v = 0; v < n; v++) {
+        core[v] = (uint32_t)(rowptr[v + 1] - rowptr[v]);
+        if (core[v] > md) md = core[v];
+    }
+    uint32_t *hist = (uint32_t *)calloc((size_t)md + 2, sizeof(uint32_t));
+    if (!prev || !flag || !next || !hist) { free(prev); free(flag); free(next); free(hist); return ORC_ENOMEM; }
+    memset(flag, 1, n);
+    uint32_t it = 0;
+    for (;;) {
+        it++;
+        memcpy(prev, core, (size_t)n * sizeof(uint32_t));
+        memset(next, 0, n);
+        int changed = 0;
+        for (uint32_t v = 0; v < n; v++) {
+            if (!flag[v] || prev[v] == 0) continue;
+            uint32_t k = hindex_of(rowptr, col, prev, v, prev[v], hist);
+            if (k != prev[v]) {
+                core[v] = k;
+                changed = 1;
+                for (int64_t e = rowptr[v]; e < rowptr[v + 1]; e++) next[col[e]] = 1;
+            }
+        }
+        if (!changed) break;
+        uint8_t *t = flag; flag = next; next = t;
+    }
+    *iters = it;
+    free(prev); free(flag); free(next); free(hist);
+    return ORC_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Level-synchronous peel of peelone.cu:157-186: `level` rises by one after a
+ * round that removed nothing, otherwise the same level is repeated (a
+ * sub-level round).  A round removes every live vertex whose residual degree
+ * equals the level at the start of the round and decrements each neighbour
+ * above the level (peelone.cu:48-87).  Degree-0 vertices have no virtual
+ * node, are never visited, and keep core 0.  *rounds = kernel launches of
+ * the reference driver, including the last one that finds nothing live.   */
+int orc_peel_rounds(uint32_t n, const int64_t *rowptr, const uint32_t *col, uint32_t *dist,
+                    uint32_t *rounds, uint32_t *kmax)
+{
+    uint8_t *done = (uint8_t *)calloc((size_t)n + 1, 1);
+    uint32_t *front = (uint32_t *)malloc((size_t)n * sizeof(uint32_t) + 4);
+    if (!done || !front) { free(done); free(front); return ORC_ENOMEM; }
+    uint64_t live = 0;
+    for (uint32_t v = 0; v < n; v++) {
+        dist[v] = (uint32_t)(rowptr[v + 1] - rowptr[v]);
+        if (dist[v] == 0) done[v] = 1; else live++;
+    }
+    uint32_t level = 0, r = 0, km = 0;
+    int plus = 1;
+    for (;;) {
+        r++;
+        if (plus) level++; else plus = 1;
+        if (live == 0) break;
+        uint32_t nf = 0;
+        for (uint32_t v = 0; v < n; v++)
+            if (!done[v] && dist[v] == level) front[nf++] = v;
+        for (uint32_t i = 0; i < nf; i++) {
+            uint32_t v = front[i];
+            done[v] = 1; live--; plus = 0;
+            if (level > km) km = level;
+            for (int64_t e = rowptr[v]; e < rowptr[v + 1]; e++) {
+                uint32_t u = col[e];
+                if (dist[u] > level) dist[u]--;
+            }
+        }
+    }
+    *rounds = r;
+    *kmax = km;
+    free(done); free(front);
+    return ORC_OK;
+}
+
+/* GPP peel of gppeel.cu:398-440: per round, scan_nodes deletes every live
+ * vertex with residual degree <= level and records final_core = level, then
+ * scatter_edges decrements each live neighbour without clamping.  Because
+ * the first level is 1, degree-0 vertices get core 1 (gppeel.cu:247-252).  */
+int orc_gpp(uint32_t n, const int64_t *rowptr, const uint32_t *col, uint32_t *final_core,
+            uint32_t *rounds)
+{
+    uint32_t *core = (uint32_t *)malloc((size_t)n * sizeof(uint32_t) + 4);
+    uint8_t *del = (uint8_t *)calloc((size_t)n + 1, 1);
+    uint32_t *front = (uint32_t *)malloc((size_t)n * sizeof(uint32_t) + 4);
+    if (!core || !del || !front) { free(core); free(del); free(front); return ORC_ENOMEM; }
+    for (uint32_t v = 0; v < n; v++) { core[v] = (uint32_t)(rowptr[v + 1] - rowptr[v]); final_core[v] = 0; }
+    uint64_t live = n;
+    uint32_t level = 0, r = 0;
+    int plus = 1;
+    for (;;) {
+        r++;
+        if (plus) level++; else plus = 1;
+        if (live == 0) break;
+        uint32_t nf = 0;
+        for (uint32_t v = 0; v < n; v++) {
+            if (del[v]) continue;
+            if (core[v] <= level) { del[v] = 1; final_core[v] = level; front[nf++] = v; plus = 0; live--; }
+        }
+        for (uint32_t i = 0; i < nf; i++) {
+            uint32_t v = front[i];
+            for (int64_t e = rowptr[v]; e < rowptr[v + 1]; e++)
+                if (!del[col[e]]) core[col[e]]--;
+        }
+    }
+    *rounds = r;
+    free(core); free(del); free(front);
+    return ORC_OK;
+}
+
+/* peelone_dyn of peelone-dyn.cc:141-158: for level = 0, 1, ... select the
+ * vertices whose residual degree equals the level, then drain a queue: each
+ * neighbour above the level is decremented and, if it lands on the level, is
+ * appended to the queue (the sub-levels run inside one launch).  Residual
+ * degrees end as core numbers; *levels = number of select/process launches
+ * (kmax + 1).                                                              */
+int orc_peel_dyn(uint32_t n, const int64_t *rowptr, const uint32_t *col, uint32_t *deg,
+                 uint32_t *levels)
+{
+    uint32_t *q = (uint32_t *)malloc((size_t)n * sizeof(uint32_t) + 4);
+    if (!q) return ORC_ENOMEM;
+    for (uint32_t v = 0; v < n; v++) deg[v] = (uint32_t)(rowptr[v + 1] - rowptr[v]);
+    uint64_t count = 0;
+    uint32_t level = 0;
+    while (count < n) {
+        uint64_t head = 0, tail = 0;
+        for (uint32_t v = 0; v < n; v++)
+            if (deg[v] == level) q[tail++] = v;
+        while (head < tail) {
+            uint32_t v = q[head++];
+            for (int64_t e = rowptr[v]; e < rowptr[v + 1]; e++) {
+                uint32_t u = col[e];
+                if (deg[u] > level) {
+                    if (--deg[u] == level) q[tail++] = u;
+                }
+            }
+        }
+        count += tail;
+        level++;
+    }
+    *levels = level;
+    free(q);
+    return ORC_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Inline-degree CSR with virtual nodes, as MakeUGraph builds it
+ * (virtual_graph.cpp:96-192): nodePointer[v] indexes a slot holding deg(v),
+ * followed by v's neighbours in edge-list order; each undirected edge i is
+ * scattered source->end then end->source.  Vertex v owns ceil(deg/part_size)
+ * virtual nodes {v, j}.  `parts` receives 2*numParts words (node, part).
+ * Degrees are computed here as in VirtualGraph::VirtualGraph (:28-44).     */
+int orc_make_ugraph(uint32_t n, uint64_t m, const uint32_t *src, const uint32_t *dst,
+                    uint32_t part_size, uint32_t *nodePointer, uint32_t *edgeList,
+                    uint32_t *parts, uint64_t *numParts)
+{
+    uint32_t *deg = (uint32_t *)calloc((size_t)n + 1, sizeof(uint32_t));
+    uint32_t *fill = (uint32_t *)calloc((size_t)n + 1, sizeof(uint32_t));
+    if (!deg || !fill) { free(deg); free(fill); return ORC_ENOMEM; }
+    for (uint64_t i = 0; i < m; i++) { deg[src[i]]++; deg[dst[i]]++; }
+    uint64_t counter = 0, np = 0;
+    for (uint32_t v = 0; v < n; v++) {
+        nodePointer[v] = (uint32_t)counter;
+        edgeList[counter] = deg[v];
+        np += (deg[v] + part_size - 1) / part_size;
+        counter += (uint64_t)deg[v] + 1;
+    }
+    for (uint64_t i = 0; i < m; i++) {
+        uint32_t s = src[i], t = dst[i];
+        edgeList[(uint64_t)nodePointer[s] + fill[s] + 1] = t; fill[s]++;
+        edgeList[(uint64_t)nodePointer[t] + fill[t] + 1] = s; fill[t]++;
+    }
+    if (parts) {
+        uint64_t c = 0;
+        for (uint32_t v = 0; v < n; v++) {
+            uint32_t k = (deg[v] + part_size - 1) / part_size;
+            for (uint32_t j = 0; j < k; j++) { parts[2 * c] = v; parts[2 * c + 1] = j; c++; }
+        }
+    }
+    *numParts = np;
+    free(deg); free(fill);
+    return ORC_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+static int cmp_u64(const void *a, const void *b)
+{
+    uint64_t x = *(const uint64_t *)a, y = *(const uint64_t *)b;
+    return (x > y) - (x < y);
+}
+
+/* De-duplicated, sorted CSR of peel/src/graph.cpp:103-131 (a std::set per
+ * vertex): both directions of every non-self-loop edge, each neighbour once,
+ * ascending.  rowptr must hold n+1 entries; col must hold 2*m entries.
+ * Returns the number of CSR entries, or -1 on allocation failure.         */
+int64_t orc_csr_dedup(uint32_t n, uint64_t m, const uint32_t *src, const uint32_t *dst,
+                      int64_t *rowptr, uint32_t *col)
+{
+    uint64_t *key = (uint64_t *)malloc((size_t)(2 * m + 1) * sizeof(uint64_t));
+    if (!key) return -1;
+    uint64_t k = 0;
+    for (uint64_t i = 0; i < m; i++) {
+        if (src[i] == dst[i]) continue;
+        key[k++] = ((uint64_t)src[i] << 32) | dst[i];
+        key[k++] = ((uint64_t)dst[i] << 32) | src[i];
+    }
+    qsort(key, (size_t)k, sizeof(uint64_t), cmp_u64);
+    for (uint32_t v = 0; v <= n; v++) rowptr[v] = 0;
+    int64_t w = 0;
+    for (uint64_t i = 0; i < k; i++) {
+        if (i > 0 && key[i] == key[i - 1]) continue;
+        rowptr[(key[i] >> 32) + 1]++;
+        col[w++] = (uint32_t)key[i];
+    }
+    for (uint32_t v = 0; v < n; v++) rowptr[v + 1] += rowptr[v];
+    free(key);
+    return w;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Local fixpoint test: for every v, at least c[v] neighbours have c >= c[v]
+ * and at most c[v] neighbours have c >= c[v]+1.  Every core vector passes;
+ * it is a cheap necessary condition used beside the BZ comparison.  Returns
+ * the number of failing vertices.                                          */
+uint64_t orc_check_local(uint32_t n, const int64_t *rowptr, const uint32_t *col, const uint32_t *c)
+{
+    uint64_t bad = 0;
+    for (uint32_t v = 0; v < n; v++) {
+        uint64_t ge = 0, gt = 0;
+        for (int64_t e = rowptr[v]; e < rowptr[v + 1]; e++) {
+            uint32_t x = c[col[e]];
+            if (x >= c[v]) ge++;
+            if (x >= c[v] + 1) gt++;
+        }
+        if (ge < c[v] || gt > c[v]) bad++;
+    }
+    return bad;
+}

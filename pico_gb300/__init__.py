@@ -1,0 +1,423 @@
+"""pico_gb300 -- GB300-native k-core decomposition engine.
+
+Python mirror of the C ABI in include/kcore.h (libkcore.so, built in-tree by
+pico_gb300/build.py).  Everything here is a thin ctypes binding: the graph
+build and every decomposition run as hand-written sm_103a CUDA inside the
+library; there is no CPU fallback.  If the library is missing the calls raise
+KCoreError instead of computing anything on the host.
+
+The reference (chriszhao13/pico) exposes no library: each method is a CUDA
+executable.  ``pico_gb300.reference`` mirrors its driver-level interface
+(``Graph(path)``, ``peelone_dyn(g)``, ``repSimulation``...) on top of this
+module.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+from dataclasses import dataclass
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "_build", "libkcore.so")
+HEADER = os.path.join(os.path.dirname(_PKG), "include", "kcore.h")
+
+# status codes (kcore.h)
+KC_OK, KC_ERR_INVALID, KC_ERR_IO, KC_ERR_CUDA, KC_ERR_NOMEM, KC_ERR_CAPACITY, KC_ERR_TIMEOUT, \
+    KC_ERR_UNSUPPORTED, KC_ERR_STATE = range(9)
+STATUS_NAMES = {0: "KC_OK", 1: "KC_ERR_INVALID", 2: "KC_ERR_IO", 3: "KC_ERR_CUDA", 4: "KC_ERR_NOMEM",
+                5: "KC_ERR_CAPACITY", 6: "KC_ERR_TIMEOUT", 7: "KC_ERR_UNSUPPORTED", 8: "KC_ERR_STATE"}
+
+# methods (kcore.h): the reference's seven drivers plus AUTO
+METHODS = {"HistoCore": 0, "CntCore": 1, "NbrCore": 2, "peelone": 3, "gppeel": 4, "peelone_dyn": 5,
+           "peel_dyn": 6, "auto": 7}
+_ALIASES = {"histo": 0, "cnt": 1, "nbr": 2, "gpp": 4, "peel": 5}
+
+LOAD_COO, LOAD_CSR_DEDUP = 0, 1
+EDGES_DEDUP, EDGES_SORT_ROWS = 1, 2
+
+
+class KCoreError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s: %s" % (STATUS_NAMES.get(code, str(code)), msg))
+        self.code = code
+
+
+class kc_stats(ctypes.Structure):
+    _fields_ = [("method", ctypes.c_uint32), ("iterations", ctypes.c_uint32), ("levels", ctypes.c_uint32),
+                ("kmax", ctypes.c_uint32), ("kmin", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+                ("n", ctypes.c_uint64), ("nnz", ctypes.c_uint64), ("ms", ctypes.c_double),
+                ("build_ms", ctypes.c_double)]
+
+
+@dataclass
+class Stats:
+    method: str
+    iterations: int
+    levels: int
+    kmax: int
+    kmin: int
+    n: int
+    nnz: int
+    ms: float
+    build_ms: float
+
+
+_lib = None
+_P = ctypes.c_void_p
+_U32P = ctypes.POINTER(ctypes.c_uint32)
+_I64P = ctypes.POINTER(ctypes.c_int64)
+_U64P = ctypes.POINTER(ctypes.c_uint64)
+
+
+def _sig(L, name, res, args):
+    f = getattr(L, name)
+    f.restype = res
+    f.argtypes = args
+
+
+def lib():
+    """Load libkcore.so (raises KCoreError when it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise KCoreError(KC_ERR_STATE, "libkcore.so is not built (%s); run pico_gb300.build.build()" % LIB_PATH)
+    L = ctypes.CDLL(LIB_PATH)
+    i, u32, u64, d = ctypes.c_int, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_double
+    PP = ctypes.POINTER(_P)
+    _sig(L, "kc_abi_version", i, [])
+    _sig(L, "kc_last_error", ctypes.c_char_p, [])
+    _sig(L, "kc_device_count", i, [])
+    _sig(L, "kc_graph_from_mtx", i, [ctypes.c_char_p, i, i, PP])
+    _sig(L, "kc_parse_mtx", i, [ctypes.c_char_p, i, _U32P, _U64P, ctypes.POINTER(_U32P), ctypes.POINTER(_U32P)])
+    _sig(L, "kc_host_free_edges", None, [_U32P, _U32P])
+    _sig(L, "kc_graph_from_edges", i, [_P, _P, u64, u32, u32, i, PP])
+    _sig(L, "kc_graph_from_edges_device", i, [_P, _P, u64, u32, u32, i, PP])
+    _sig(L, "kc_graph_from_csr", i, [_P, _P, u32, i, PP])
+    _sig(L, "kc_graph_from_csr_device", i, [_P, _P, u32, i, PP])
+    _sig(L, "kc_graph_validate", i, [_P, _U64P])
+    _sig(L, "kc_graph_free", i, [_P])
+    _sig(L, "kc_graph_info", i, [_P, _U32P, _U64P, _U32P, _U64P])
+    _sig(L, "kc_graph_device_csr", i, [_P, PP, PP])
+    _sig(L, "kc_graph_copy_csr", i, [_P, _P, _P])
+    _sig(L, "kc_graph_degrees", i, [_P, _P])
+    _sig(L, "kc_graph_virtual_layout", i, [_P, u32, _P, _P, _P, _U64P])
+    _sig(L, "kc_decompose", i, [_P, i, _P, i, ctypes.POINTER(kc_stats), _P])
+    _sig(L, "kc_graph_device_core", i, [_P, PP])
+    _sig(L, "kc_graph_last_timing", i, [_P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)])
+    _sig(L, "kc_host_alloc", i, [PP, ctypes.c_size_t])
+    _sig(L, "kc_host_free", i, [_P])
+    _sig(L, "kc_device_alloc", i, [PP, ctypes.c_size_t, i])
+    _sig(L, "kc_device_free", i, [_P])
+    _sig(L, "kc_memcpy", i, [_P, _P, ctypes.c_size_t, i])
+    _sig(L, "kc_device_synchronize", i, [i])
+    _sig(L, "kc_gen_rmat", i, [u32, u64, d, d, d, u64, _P, _P, _P])
+    _sig(L, "kc_gen_er", i, [u32, u64, u64, _P, _P, _P])
+    _sig(L, "kc_gen_planted", i, [u32, u32, d, u64, _P, _P, u64, _U64P, _P])
+    _lib = L
+    return L
+
+
+def check(rc):
+    if rc != KC_OK:
+        raise KCoreError(rc, lib().kc_last_error().decode(errors="replace"))
+
+
+def header_symbols(path=HEADER):
+    """Names of the functions declared in include/kcore.h."""
+    txt = open(path).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(kc_\w+)\s*\(", txt)))
+
+
+def method_id(method) -> int:
+    if isinstance(method, int):
+        return method
+    if method in METHODS:
+        return METHODS[method]
+    m = method.lower()
+    for k, v in METHODS.items():
+        if k.lower() == m:
+            return v
+    if m in _ALIASES:
+        return _ALIASES[m]
+    raise ValueError("unknown method %r" % (method,))
+
+
+def method_name(mid: int) -> str:
+    for k, v in METHODS.items():
+        if v == mid:
+            return k
+    return str(mid)
+
+
+def device_count() -> int:
+    return lib().kc_device_count()
+
+
+def _ptr(a):
+    return ctypes.c_void_p(a.ctypes.data) if a is not None and a.size else ctypes.c_void_p(0)
+
+
+class DeviceBuffer:
+    """Device memory owned by Python (kc_device_alloc / kc_device_free)."""
+
+    def __init__(self, nbytes, device=0):
+        p = ctypes.c_void_p()
+        check(lib().kc_device_alloc(ctypes.byref(p), max(int(nbytes), 1), device))
+        self.ptr = p.value
+        self.nbytes = int(nbytes)
+        self.device = device
+
+    def free(self):
+        if self.ptr:
+            lib().kc_device_free(ctypes.c_void_p(self.ptr))
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    def upload(self, arr):
+        arr = np.ascontiguousarray(arr)
+        assert arr.nbytes <= self.nbytes
+        check(lib().kc_memcpy(ctypes.c_void_p(self.ptr), _ptr(arr), arr.nbytes, 1))
+
+    def download(self, dtype, count):
+        out = np.empty(count, dtype=dtype)
+        if out.nbytes:
+            check(lib().kc_memcpy(_ptr(out), ctypes.c_void_p(self.ptr), out.nbytes, 2))
+        return out
+
+
+class Graph:
+    """A device-resident graph (owns a kc_graph handle)."""
+
+    def __init__(self, handle, device=0):
+        self._h = ctypes.c_void_p(handle)
+        self.device = device
+        n, nnz, md, vn = ctypes.c_uint32(), ctypes.c_uint64(), ctypes.c_uint32(), ctypes.c_uint64()
+        check(lib().kc_graph_info(self._h, ctypes.byref(n), ctypes.byref(nnz), ctypes.byref(md), ctypes.byref(vn)))
+        self.n, self.nnz, self.max_degree, self.num_vnodes = n.value, nnz.value, md.value, vn.value
+
+    # ---- construction ----
+    @classmethod
+    def from_mtx(cls, path, mode="coo", device=0):
+        m = {"coo": LOAD_COO, "csr": LOAD_CSR_DEDUP, "dedup": LOAD_CSR_DEDUP}.get(mode, mode)
+        h = ctypes.c_void_p()
+        check(lib().kc_graph_from_mtx(os.fsencode(path), m, device, ctypes.byref(h)))
+        return cls(h.value, device)
+
+    @classmethod
+    def from_edges(cls, src, dst, n, dedup=False, sort_rows=False, device=0):
+        src = np.ascontiguousarray(src, dtype=np.uint32)
+        dst = np.ascontiguousarray(dst, dtype=np.uint32)
+        flags = (EDGES_DEDUP if dedup else 0) | (EDGES_SORT_ROWS if sort_rows else 0)
+        h = ctypes.c_void_p()
+        check(lib().kc_graph_from_edges(_ptr(src), _ptr(dst), src.size, int(n), flags, device, ctypes.byref(h)))
+        return cls(h.value, device)
+
+    @classmethod
+    def from_edges_device(cls, d_src, d_dst, m, n, dedup=False, sort_rows=False, device=0):
+        flags = (EDGES_DEDUP if dedup else 0) | (EDGES_SORT_ROWS if sort_rows else 0)
+        h = ctypes.c_void_p()
+        check(lib().kc_graph_from_edges_device(ctypes.c_void_p(d_src), ctypes.c_void_p(d_dst), int(m), int(n),
+                                               flags, device, ctypes.byref(h)))
+        return cls(h.value, device)
+
+    @classmethod
+    def from_csr(cls, rowptr, col, device=0):
+        rowptr = np.ascontiguousarray(rowptr, dtype=np.int64)
+        col = np.ascontiguousarray(col, dtype=np.uint32)
+        h = ctypes.c_void_p()
+        check(lib().kc_graph_from_csr(_ptr(rowptr), _ptr(col), rowptr.size - 1, device, ctypes.byref(h)))
+        return cls(h.value, device)
+
+    @classmethod
+    def from_csr_ptr(cls, rowptr_ptr, col_ptr, n, device=0):
+        """Host pointers (e.g. pinned buffers) to a CSR; copies H2D inside the call."""
+        h = ctypes.c_void_p()
+        check(lib().kc_graph_from_csr(ctypes.c_void_p(rowptr_ptr), ctypes.c_void_p(col_ptr), int(n), device,
+                                      ctypes.byref(h)))
+        return cls(h.value, device)
+
+    # ---- lifetime ----
+    def free(self):
+        if self._h is not None and self._h.value:
+            lib().kc_graph_free(self._h)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.free()
+
+    @property
+    def handle(self):
+        return self._h
+
+    # ---- queries ----
+    def csr(self):
+        rowptr = np.empty(self.n + 1, dtype=np.int64)
+        col = np.empty(max(self.nnz, 1), dtype=np.uint32)
+        check(lib().kc_graph_copy_csr(self._h, _ptr(rowptr), _ptr(col)))
+        return rowptr, col[:self.nnz]
+
+    def degrees(self):
+        d = np.empty(max(self.n, 1), dtype=np.uint32)
+        check(lib().kc_graph_degrees(self._h, _ptr(d)))
+        return d[:self.n]
+
+    def device_csr(self):
+        r, c = ctypes.c_void_p(), ctypes.c_void_p()
+        check(lib().kc_graph_device_csr(self._h, ctypes.byref(r), ctypes.byref(c)))
+        return r.value, c.value
+
+    def validate(self):
+        bad = ctypes.c_uint64()
+        check(lib().kc_graph_validate(self._h, ctypes.byref(bad)))
+        return bad.value
+
+    def virtual_layout(self, part_size=64):
+        """Reference virtual-graph layout (nodePointer, edgeList, parts[numParts, 2])."""
+        np_ = ctypes.c_uint64()
+        check(lib().kc_graph_virtual_layout(self._h, part_size, None, None, None, ctypes.byref(np_)))
+        k = np_.value
+        node_ptr = np.empty(max(self.n, 1), dtype=np.uint32)
+        edge_list = np.empty(max(self.nnz + self.n, 1), dtype=np.uint32)
+        parts = np.empty(max(2 * k, 2), dtype=np.uint32)
+        check(lib().kc_graph_virtual_layout(self._h, part_size, _ptr(node_ptr), _ptr(edge_list), _ptr(parts),
+                                            ctypes.byref(np_)))
+        return node_ptr[:self.n], edge_list[:self.nnz + self.n], parts[:2 * k].reshape(k, 2)
+
+    # ---- decomposition ----
+    def decompose(self, method="peelone_dyn", out=None, stream=0):
+        """Core numbers (uint32[n]) and Stats.  `out`: optional host array to fill."""
+        mid = method_id(method)
+        core = out if out is not None else np.empty(max(self.n, 1), dtype=np.uint32)
+        st = kc_stats()
+        check(lib().kc_decompose(self._h, mid, _ptr(core), 0, ctypes.byref(st), ctypes.c_void_p(stream)))
+        return core[:self.n], _stats(st)
+
+    def decompose_device(self, method="peelone_dyn", stream=0, stats=False):
+        """Run on the device and leave the result there; returns Stats (if asked)."""
+        st = kc_stats()
+        check(lib().kc_decompose(self._h, method_id(method), None, 0, ctypes.byref(st) if stats else None,
+                                 ctypes.c_void_p(stream)))
+        return _stats(st) if stats else None
+
+    def last_timing(self):
+        """(total_ms, kernel_ms) of the last decomposition (CUDA events)."""
+        a, b = ctypes.c_double(), ctypes.c_double()
+        check(lib().kc_graph_last_timing(self._h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    def device_core(self):
+        p = ctypes.c_void_p()
+        check(lib().kc_graph_device_core(self._h, ctypes.byref(p)))
+        return p.value
+
+
+def _stats(st):
+    return Stats(method=method_name(st.method), iterations=st.iterations, levels=st.levels, kmax=st.kmax,
+                 kmin=st.kmin, n=st.n, nnz=st.nnz, ms=st.ms, build_ms=st.build_ms)
+
+
+def parse_mtx(path, mode="coo"):
+    """Host-only MatrixMarket parse: (n, src uint32[m], dst uint32[m])."""
+    m_ = {"coo": LOAD_COO, "csr": LOAD_CSR_DEDUP, "dedup": LOAD_CSR_DEDUP}.get(mode, mode)
+    n, m = ctypes.c_uint32(), ctypes.c_uint64()
+    s, d = _U32P(), _U32P()
+    check(lib().kc_parse_mtx(os.fsencode(path), m_, ctypes.byref(n), ctypes.byref(m), ctypes.byref(s),
+                             ctypes.byref(d)))
+    try:
+        cnt = m.value
+        src = np.ctypeslib.as_array(s, shape=(max(cnt, 1),))[:cnt].copy()
+        dst = np.ctypeslib.as_array(d, shape=(max(cnt, 1),))[:cnt].copy()
+    finally:
+        lib().kc_host_free_edges(s, d)
+    return n.value, src, dst
+
+
+# ---- generators (device) ----
+RMAT_ABC = (0.57, 0.19, 0.19)
+
+
+def gen_rmat_edges(scale, num_edges, seed, abc=RMAT_ABC, device=0):
+    """Raw R-MAT edge list on the device: (DeviceBuffer src, DeviceBuffer dst, m)."""
+    s = DeviceBuffer(4 * num_edges, device)
+    d = DeviceBuffer(4 * num_edges, device)
+    check(lib().kc_gen_rmat(scale, num_edges, abc[0], abc[1], abc[2], seed, ctypes.c_void_p(s.ptr),
+                            ctypes.c_void_p(d.ptr), None))
+    check(lib().kc_device_synchronize(device))
+    return s, d, num_edges
+
+
+def gen_er_edges(n, m, seed, device=0):
+    s = DeviceBuffer(4 * m, device)
+    d = DeviceBuffer(4 * m, device)
+    check(lib().kc_gen_er(n, m, seed, ctypes.c_void_p(s.ptr), ctypes.c_void_p(d.ptr), None))
+    check(lib().kc_device_synchronize(device))
+    return s, d, m
+
+
+def gen_planted_edges(n, k, p, seed, device=0):
+    cap = int(k * (k - 1) // 2 * min(1.0, p * 1.1 + 0.01)) + 1024
+    s = DeviceBuffer(4 * cap, device)
+    d = DeviceBuffer(4 * cap, device)
+    m = ctypes.c_uint64()
+    check(lib().kc_gen_planted(n, k, p, seed, ctypes.c_void_p(s.ptr), ctypes.c_void_p(d.ptr), cap,
+                               ctypes.byref(m), None))
+    check(lib().kc_device_synchronize(device))
+    return s, d, m.value
+
+
+def rmat_graph(scale, edge_factor, seed, abc=RMAT_ABC, device=0):
+    """R-MAT graph: 2^scale ids, edge_factor*2^scale draws, deduplicated, symmetrised."""
+    n = 1 << scale
+    s, d, m = gen_rmat_edges(scale, edge_factor * n, seed, abc, device)
+    g = Graph.from_edges_device(s.ptr, d.ptr, m, n, dedup=True, device=device)
+    s.free()
+    d.free()
+    return g
+
+
+def er_graph(n, m, seed, device=0):
+    """Erdos-Renyi G(n, m): m distinct edges drawn without replacement."""
+    s, d, mm = gen_er_edges(n, m, seed, device)
+    g = Graph.from_edges_device(s.ptr, d.ptr, mm, n, dedup=True, device=device)
+    s.free()
+    d.free()
+    return g
+
+
+def rmat_planted_graph(scale, edge_factor, k, p, seed, abc=RMAT_ABC, device=0):
+    """R-MAT graph plus a planted dense subgraph of k vertices at edge probability p."""
+    n = 1 << scale
+    m1 = edge_factor * n
+    s1, d1, _ = gen_rmat_edges(scale, m1, seed, abc, device)
+    s2, d2, m2 = gen_planted_edges(n, k, p, seed + 1, device)
+    s = DeviceBuffer(4 * (m1 + m2), device)
+    d = DeviceBuffer(4 * (m1 + m2), device)
+    for dst_buf, a, b in ((s, s1, s2), (d, d1, d2)):
+        check(lib().kc_memcpy(ctypes.c_void_p(dst_buf.ptr), ctypes.c_void_p(a.ptr), 4 * m1, 3))
+        if m2:
+            check(lib().kc_memcpy(ctypes.c_void_p(dst_buf.ptr + 4 * m1), ctypes.c_void_p(b.ptr), 4 * m2, 3))
+    for b in (s1, d1, s2, d2):
+        b.free()
+    g = Graph.from_edges_device(s.ptr, d.ptr, m1 + m2, n, dedup=True, device=device)
+    s.free()
+    d.free()
+    return g

@@ -1,0 +1,452 @@
+// C ABI of libkcore.so: graph handles, decomposition dispatch, generators.
+// See include/kcore.h for the contract of each entry point.
+#include <algorithm>
+#include <cstdarg>
+#include <cstring>
+#include <string>
+
+#include "kc_device.cuh"
+#include "kc_internal.h"
+
+namespace kc {
+
+static thread_local std::string g_last_error;
+
+int fail(int code, const char *fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+void clear_error() { g_last_error.clear(); }
+
+int dmalloc(void **p, size_t bytes, const char *what) {
+    *p = nullptr;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *p = nullptr;
+        return fail(KC_ERR_NOMEM, "cudaMalloc(%zu bytes) for %s: %s", bytes, what, cudaGetErrorString(e));
+    }
+    return KC_OK;
+}
+
+void dfree(void *p) {
+    if (p) cudaFree(p);
+}
+
+Graph::~Graph() {
+    int cur = 0;
+    cudaGetDevice(&cur);
+    cudaSetDevice(device);
+    dfree(rowptr);
+    dfree(col);
+    dfree(core);
+    dfree(bitmap);
+    dfree(alive);
+    dfree(gq);
+    dfree(peel_ctl);
+    for (int i = 0; i < 2; i++) {
+        dfree(list[i]);
+        dfree(big[i]);
+    }
+    dfree(hctl);
+    dfree(red);
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    if (evk0) cudaEventDestroy(evk0);
+    if (evk1) cudaEventDestroy(evk1);
+    if (stream) cudaStreamDestroy(stream);
+    cudaSetDevice(cur);
+}
+
+static int open_device(int device) {
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        return fail(KC_ERR_CUDA, "no CUDA device available (%s)", cudaGetErrorString(e));
+    }
+    if (device < 0 || device >= count) return fail(KC_ERR_INVALID, "device %d out of range (%d devices)", device, count);
+    KC_CUDA(cudaSetDevice(device));
+    return KC_OK;
+}
+
+static int new_graph(int device, kc_graph **out) {
+    KC_TRY(open_device(device));
+    kc_graph *g = new (std::nothrow) kc_graph();
+    if (!g) return fail(KC_ERR_NOMEM, "host allocation of graph handle");
+    g->device = device;
+    cudaDeviceGetAttribute(&g->sm_count, cudaDevAttrMultiProcessorCount, device);
+    cudaError_t e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete g;
+        return fail(KC_ERR_CUDA, "stream create: %s", cudaGetErrorString(e));
+    }
+    *out = g;
+    return KC_OK;
+}
+
+__global__ void core_minmax(const uint32_t *__restrict__ c, uint32_t n, uint32_t *mm) {
+    uint32_t mn = 0xffffffffu, mx = 0;
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n; v += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t x = c[v];
+        mn = min(mn, x);
+        mx = max(mx, x);
+    }
+    mn = __reduce_min_sync(KC_FULL_MASK, mn);
+    mx = __reduce_max_sync(KC_FULL_MASK, mx);
+    if ((threadIdx.x & 31) == 0) {
+        atomicMin(&mm[0], mn);
+        atomicMax(&mm[1], mx);
+    }
+}
+
+}  // namespace kc
+
+using namespace kc;
+
+extern "C" {
+
+int kc_abi_version(void) { return KC_ABI_VERSION; }
+
+const char *kc_last_error(void) { return g_last_error.c_str(); }
+
+int kc_device_count(void) {
+    int c = 0;
+    if (cudaGetDeviceCount(&c) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return c;
+}
+
+int kc_parse_mtx(const char *path, int mode, uint32_t *n, uint64_t *m, uint32_t **src, uint32_t **dst) {
+    clear_error();
+    return parse_mtx(path, mode, n, m, src, dst);
+}
+
+void kc_host_free_edges(uint32_t *src, uint32_t *dst) {
+    free(src);
+    free(dst);
+}
+
+int kc_graph_from_edges_device(const uint32_t *d_src, const uint32_t *d_dst, uint64_t m, uint32_t n, uint32_t flags,
+                               int device, kc_graph **out) {
+    clear_error();
+    if (!out || (m && (!d_src || !d_dst))) return fail(KC_ERR_INVALID, "null argument");
+    *out = nullptr;
+    kc_graph *g = nullptr;
+    KC_TRY(new_graph(device, &g));
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    cudaEventRecord(a, g->stream);
+    int rc = build_csr_from_edges(g, d_src, d_dst, m, n, flags);
+    cudaEventRecord(b, g->stream);
+    cudaEventSynchronize(b);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (rc) {
+        delete g;
+        return rc;
+    }
+    if (g->max_deg >= 0x7fffffffu) {
+        delete g;
+        return fail(KC_ERR_UNSUPPORTED, "degree above 2^31-1");
+    }
+    g->build_ms = ms;
+    *out = g;
+    return KC_OK;
+}
+
+int kc_graph_from_edges(const uint32_t *src, const uint32_t *dst, uint64_t m, uint32_t n, uint32_t flags, int device,
+                        kc_graph **out) {
+    clear_error();
+    if (!out || (m && (!src || !dst))) return fail(KC_ERR_INVALID, "null argument");
+    *out = nullptr;
+    KC_TRY(open_device(device));
+    uint32_t *ds = nullptr, *dd = nullptr;
+    KC_TRY(dalloc(&ds, std::max<uint64_t>(m, 1), "edge sources"));
+    int rc = dalloc(&dd, std::max<uint64_t>(m, 1), "edge targets");
+    if (rc) { dfree(ds); return rc; }
+    if (m) {
+        cudaError_t e1 = cudaMemcpy(ds, src, m * 4, cudaMemcpyHostToDevice);
+        cudaError_t e2 = cudaMemcpy(dd, dst, m * 4, cudaMemcpyHostToDevice);
+        if (e1 != cudaSuccess || e2 != cudaSuccess) {
+            dfree(ds);
+            dfree(dd);
+            return fail(KC_ERR_CUDA, "edge upload: %s", cudaGetErrorString(e1 != cudaSuccess ? e1 : e2));
+        }
+    }
+    rc = kc_graph_from_edges_device(ds, dd, m, n, flags, device, out);
+    dfree(ds);
+    dfree(dd);
+    return rc;
+}
+
+int kc_graph_from_mtx(const char *path, int mode, int device, kc_graph **out) {
+    clear_error();
+    uint32_t n = 0, *src = nullptr, *dst = nullptr;
+    uint64_t m = 0;
+    KC_TRY(parse_mtx(path, mode, &n, &m, &src, &dst));
+    int rc = kc_graph_from_edges(src, dst, m, n, mode == KC_LOAD_CSR_DEDUP ? KC_EDGES_DEDUP : 0u, device, out);
+    free(src);
+    free(dst);
+    return rc;
+}
+
+static int from_csr_common(const int64_t *rowptr, const uint32_t *col, uint32_t n, int device, kc_graph **out,
+                           cudaMemcpyKind kind) {
+    if (!out || !rowptr) return fail(KC_ERR_INVALID, "null argument");
+    *out = nullptr;
+    kc_graph *g = nullptr;
+    KC_TRY(new_graph(device, &g));
+    int64_t nnz = 0;
+    cudaError_t e = cudaMemcpy(&nnz, rowptr + n, 8, kind == cudaMemcpyHostToDevice ? cudaMemcpyHostToHost : cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) { delete g; return fail(KC_ERR_CUDA, "read rowptr[n]: %s", cudaGetErrorString(e)); }
+    if (nnz < 0 || (nnz > 0 && !col)) { delete g; return fail(KC_ERR_INVALID, "bad rowptr[n] = %lld", (long long)nnz); }
+    g->n = n;
+    g->nnz = (uint64_t)nnz;
+    int rc = dalloc(&g->rowptr, (uint64_t)n + 1, "row offsets");
+    if (!rc) rc = dalloc(&g->col, g->nnz + 1, "column ids");
+    if (rc) { delete g; return rc; }
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    cudaEventRecord(a, g->stream);
+    cudaMemcpyAsync(g->rowptr, rowptr, ((uint64_t)n + 1) * 8, kind, g->stream);
+    if (nnz) cudaMemcpyAsync(g->col, col, g->nnz * 4, kind, g->stream);
+    cudaEventRecord(b, g->stream);
+    e = cudaEventSynchronize(b);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (e != cudaSuccess) { delete g; return fail(KC_ERR_CUDA, "CSR upload: %s", cudaGetErrorString(e)); }
+    rc = graph_finish(g);
+    if (rc) { delete g; return rc; }
+    if (g->max_deg >= 0x7fffffffu) { delete g; return fail(KC_ERR_UNSUPPORTED, "degree above 2^31-1"); }
+    g->build_ms = ms;
+    *out = g;
+    return KC_OK;
+}
+
+int kc_graph_from_csr(const int64_t *rowptr, const uint32_t *col, uint32_t n, int device, kc_graph **out) {
+    clear_error();
+    return from_csr_common(rowptr, col, n, device, out, cudaMemcpyHostToDevice);
+}
+
+int kc_graph_from_csr_device(const int64_t *d_rowptr, const uint32_t *d_col, uint32_t n, int device, kc_graph **out) {
+    clear_error();
+    return from_csr_common(d_rowptr, d_col, n, device, out, cudaMemcpyDeviceToDevice);
+}
+
+int kc_graph_validate(kc_graph *g, uint64_t *bad) {
+    clear_error();
+    if (!g || !bad) return fail(KC_ERR_INVALID, "null argument");
+    KC_CUDA(cudaSetDevice(g->device));
+    return graph_validate(g, bad);
+}
+
+int kc_graph_free(kc_graph *g) {
+    clear_error();
+    if (!g) return KC_OK;
+    delete g;
+    return KC_OK;
+}
+
+int kc_graph_info(const kc_graph *g, uint32_t *n, uint64_t *nnz, uint32_t *max_degree, uint64_t *num_vnodes) {
+    clear_error();
+    if (!g) return fail(KC_ERR_INVALID, "null graph");
+    if (n) *n = g->n;
+    if (nnz) *nnz = g->nnz;
+    if (max_degree) *max_degree = g->max_deg;
+    if (num_vnodes) *num_vnodes = g->num_vnodes;
+    return KC_OK;
+}
+
+int kc_graph_device_csr(const kc_graph *g, const int64_t **d_rowptr, const uint32_t **d_col) {
+    clear_error();
+    if (!g) return fail(KC_ERR_INVALID, "null graph");
+    if (d_rowptr) *d_rowptr = g->rowptr;
+    if (d_col) *d_col = g->col;
+    return KC_OK;
+}
+
+int kc_graph_copy_csr(const kc_graph *g, int64_t *rowptr, uint32_t *col) {
+    clear_error();
+    if (!g) return fail(KC_ERR_INVALID, "null graph");
+    KC_CUDA(cudaSetDevice(g->device));
+    if (rowptr) KC_CUDA(cudaMemcpy(rowptr, g->rowptr, ((uint64_t)g->n + 1) * 8, cudaMemcpyDeviceToHost));
+    if (col && g->nnz) KC_CUDA(cudaMemcpy(col, g->col, g->nnz * 4, cudaMemcpyDeviceToHost));
+    return KC_OK;
+}
+
+__global__ void degrees_kernel(const int64_t *__restrict__ rowptr, uint32_t n, uint32_t *deg) {
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n; v += (uint64_t)gridDim.x * blockDim.x)
+        deg[v] = (uint32_t)(rowptr[v + 1] - rowptr[v]);
+}
+
+int kc_graph_degrees(const kc_graph *g, uint32_t *deg) {
+    clear_error();
+    if (!g || !deg) return fail(KC_ERR_INVALID, "null argument");
+    KC_CUDA(cudaSetDevice(g->device));
+    if (!g->n) return KC_OK;
+    uint32_t *d = nullptr;
+    KC_TRY(dalloc(&d, g->n, "degrees"));
+    degrees_kernel<<<std::max(1, std::min<int>(g->sm_count * 8, (int)((g->n + 255) / 256))), 256, 0, g->stream>>>(
+        g->rowptr, g->n, d);
+    cudaError_t e = cudaMemcpyAsync(deg, d, (uint64_t)g->n * 4, cudaMemcpyDeviceToHost, g->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    dfree(d);
+    if (e != cudaSuccess) return fail(KC_ERR_CUDA, "degrees: %s", cudaGetErrorString(e));
+    return KC_OK;
+}
+
+int kc_graph_virtual_layout(kc_graph *g, uint32_t part_size, uint32_t *node_pointer, uint32_t *edge_list,
+                            uint32_t *parts, uint64_t *num_parts) {
+    clear_error();
+    if (!g || !num_parts) return fail(KC_ERR_INVALID, "null argument");
+    KC_CUDA(cudaSetDevice(g->device));
+    return virtual_layout(g, part_size, node_pointer, edge_list, parts, num_parts);
+}
+
+int kc_decompose(kc_graph *g, int method, uint32_t *core_out, int out_on_device, kc_stats *stats, void *stream) {
+    clear_error();
+    if (!g) return fail(KC_ERR_INVALID, "null graph");
+    if (method < KC_HISTO || method > KC_AUTO) return fail(KC_ERR_INVALID, "unknown method %d", method);
+    KC_CUDA(cudaSetDevice(g->device));
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : g->stream;
+    kc_stats st;
+    memset(&st, 0, sizeof(st));
+    int run = method == KC_AUTO ? KC_PEELONE_DYN : method;
+    st.method = (uint32_t)run;
+    st.n = g->n;
+    st.nnz = g->nnz;
+    st.build_ms = g->build_ms;
+    int rc;
+    if (g->n == 0) {
+        rc = KC_OK;
+        if (!g->core) KC_TRY(dalloc(&g->core, 1, "core"));
+        g->core_valid = true;
+    } else if (run == KC_HISTO || run == KC_CNT || run == KC_NBR) {
+        rc = hindex_run(g, s, &st);
+    } else {
+        rc = peel_run(g, s, run == KC_GPP, &st);
+    }
+    if (rc) return rc;
+    if (stats) {
+        // Max K / Min K as utility::PrintMaxMin reports them (util.cpp:6-22):
+        // the minimum starts at 10, so it never exceeds 10.
+        if (!g->red) KC_TRY(dalloc(&g->red, 2, "reduction"));
+        uint32_t init[2] = {10u, 0u};
+        KC_CUDA(cudaMemcpyAsync(g->red, init, 8, cudaMemcpyHostToDevice, s));
+        if (g->n)
+            core_minmax<<<std::max(1, std::min<int>(g->sm_count * 4, (int)((g->n + 255) / 256))), 256, 0, s>>>(
+                g->core, g->n, g->red);
+        uint32_t mm[2];
+        KC_CUDA(cudaMemcpyAsync(mm, g->red, 8, cudaMemcpyDeviceToHost, s));
+        KC_CUDA(cudaStreamSynchronize(s));
+        st.kmin = mm[0];
+        st.kmax = mm[1];
+        *stats = st;
+    }
+    if (core_out && g->n) {
+        KC_CUDA(cudaMemcpyAsync(core_out, g->core, (uint64_t)g->n * 4,
+                                out_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
+        KC_CUDA(cudaStreamSynchronize(s));
+    }
+    return KC_OK;
+}
+
+int kc_graph_last_timing(const kc_graph *g, double *total_ms, double *kernel_ms) {
+    clear_error();
+    if (!g) return fail(KC_ERR_INVALID, "null graph");
+    if (total_ms) *total_ms = g->last_ms;
+    if (kernel_ms) *kernel_ms = g->last_kernel_ms;
+    return KC_OK;
+}
+
+int kc_graph_device_core(const kc_graph *g, const uint32_t **d_core) {
+    clear_error();
+    if (!g || !d_core) return fail(KC_ERR_INVALID, "null argument");
+    if (!g->core_valid) return fail(KC_ERR_STATE, "no decomposition has completed on this graph");
+    *d_core = g->core;
+    return KC_OK;
+}
+
+int kc_host_alloc(void **p, size_t bytes) {
+    clear_error();
+    if (!p) return fail(KC_ERR_INVALID, "null argument");
+    cudaError_t e = cudaMallocHost(p, bytes ? bytes : 1);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *p = nullptr;
+        return fail(KC_ERR_NOMEM, "cudaMallocHost(%zu): %s", bytes, cudaGetErrorString(e));
+    }
+    return KC_OK;
+}
+
+int kc_host_free(void *p) {
+    clear_error();
+    if (p) KC_CUDA(cudaFreeHost(p));
+    return KC_OK;
+}
+
+int kc_device_alloc(void **p, size_t bytes, int device) {
+    clear_error();
+    if (!p) return fail(KC_ERR_INVALID, "null argument");
+    KC_TRY(open_device(device));
+    return dmalloc(p, bytes ? bytes : 1, "kc_device_alloc");
+}
+
+int kc_device_free(void *p) {
+    clear_error();
+    if (p) KC_CUDA(cudaFree(p));
+    return KC_OK;
+}
+
+int kc_memcpy(void *dst, const void *src, size_t bytes, int kind) {
+    clear_error();
+    if (!bytes) return KC_OK;
+    if (!dst || !src) return fail(KC_ERR_INVALID, "null argument");
+    cudaMemcpyKind k = kind == 1 ? cudaMemcpyHostToDevice
+                                 : (kind == 2 ? cudaMemcpyDeviceToHost : (kind == 3 ? cudaMemcpyDeviceToDevice : cudaMemcpyDefault));
+    if (kind < 1 || kind > 3) return fail(KC_ERR_INVALID, "copy kind %d", kind);
+    KC_CUDA(cudaMemcpy(dst, src, bytes, k));
+    return KC_OK;
+}
+
+int kc_device_synchronize(int device) {
+    clear_error();
+    KC_TRY(open_device(device));
+    KC_CUDA(cudaDeviceSynchronize());
+    return KC_OK;
+}
+
+int kc_gen_rmat(uint32_t scale, uint64_t num_edges, double a, double b, double c, uint64_t seed, uint32_t *d_src,
+                uint32_t *d_dst, void *stream) {
+    clear_error();
+    return gen_rmat(scale, num_edges, a, b, c, seed, d_src, d_dst, static_cast<cudaStream_t>(stream));
+}
+
+int kc_gen_er(uint32_t n, uint64_t m, uint64_t seed, uint32_t *d_src, uint32_t *d_dst, void *stream) {
+    clear_error();
+    return gen_er(n, m, seed, d_src, d_dst, static_cast<cudaStream_t>(stream));
+}
+
+int kc_gen_planted(uint32_t n, uint32_t k, double p, uint64_t seed, uint32_t *d_src, uint32_t *d_dst, uint64_t cap,
+                   uint64_t *m, void *stream) {
+    clear_error();
+    if (!m) return fail(KC_ERR_INVALID, "null argument");
+    return gen_planted(n, k, p, seed, d_src, d_dst, cap, m, static_cast<cudaStream_t>(stream));
+}
+
+}  // extern "C"

@@ -1,0 +1,395 @@
+// h-index iteration: the k-core path of HistoCore / CntCore / NbrCore
+// (index2core/HistoCore.cu:15-202,292-341; CntCore.cu:17-264,344-417;
+// NbrCore.cu:12-167,244-297) as one cooperative launch.
+//
+// Every vertex starts at its degree; a sweep replaces the estimate c[v] of each
+// active vertex by the h-index of its neighbours' estimates (the largest k
+// with at least k neighbours at >= k), which never exceeds c[v].  Estimates
+// stay upper bounds of the core numbers and the iteration stops at the
+// largest fixpoint, which is the core vector.  The reference runs three
+// trigger schemes for the same operator (persistent per-vertex histograms,
+// support counters, neighbour flags), each as several launches plus a
+// blocking flag copy per iteration.  Here:
+//   * a vertex is re-examined only when a neighbour's estimate dropped from
+//     above its own (neighbour notification, deduplicated by a bitmap), so
+//     settled vertices read nothing;
+//   * the support test "at least c[v] neighbours at >= c[v]" runs first and
+//     settles most re-examined vertices without a histogram (the support
+//     counter of CntCore.cu:258-261 / the top bin of HistoCore.cu:184-198);
+//   * otherwise the h-index comes from a degree-capped histogram built in
+//     shared memory (one warp per vertex up to 512 neighbours; above that one
+//     CTA narrows the value range with 4096-bin passes until bins are one
+//     value wide) and a warp-shuffle suffix scan;
+//   * updates are visible at once within a sweep (Gauss-Seidel), which only
+//     shortens the trajectory; sweeps are separated by a grid barrier with a
+//     bounded wait.
+#include <algorithm>
+
+#include "kc_device.cuh"
+#include "kc_internal.h"
+
+namespace kc {
+
+constexpr int HX_THREADS = 512;
+constexpr int HX_WARPS = HX_THREADS / 32;
+constexpr uint32_t HX_WARP_MAX = 512;   // rows up to this length: one warp
+constexpr uint32_t HX_BINS = 4096;      // CTA histogram bins
+
+struct HxArgs {
+    const int64_t *rowptr;
+    const uint32_t *col;
+    uint32_t n;
+    uint32_t *c;
+    uint32_t *inlist;  // bitmap: vertex queued for the next sweep
+    uint32_t *list[2];
+    uint32_t *big[2];
+    HindexCtl *ctl;
+    unsigned long long timeout_ns;
+    uint32_t max_sweeps;
+};
+
+__global__ void hindex_init(const int64_t *__restrict__ rowptr, uint32_t n, uint32_t *c, uint32_t *inlist,
+                            uint32_t *big0, HindexCtl *ctl) {
+    const unsigned lane = threadIdx.x & 31;
+    uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t base = blockIdx.x * (uint64_t)blockDim.x; base < n; base += stride) {
+        uint64_t v = base + threadIdx.x;
+        bool bigv = false;
+        if (v < n) {
+            uint32_t d = (uint32_t)(rowptr[v + 1] - rowptr[v]);
+            c[v] = d;
+            bigv = d > HX_WARP_MAX;
+        }
+        unsigned b = __ballot_sync(KC_FULL_MASK, bigv);
+        if (b) {
+            unsigned long long p = 0;
+            if (lane == 0) p = atomicAdd(&ctl->big_len[0], (unsigned long long)__popc(b));
+            p = __shfl_sync(KC_FULL_MASK, p, 0);
+            if (bigv) big0[p + __popc(b & ((1u << lane) - 1u))] = (uint32_t)v;
+        }
+    }
+    uint64_t words = ((uint64_t)n + 31) / 32;
+    for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < words; w += stride) inlist[w] = 0u;
+}
+
+// Queue u for the next sweep unless it is queued already.
+__device__ __forceinline__ void hx_activate(const HxArgs &A, uint32_t u, unsigned nxt) {
+    unsigned bit = 1u << (u & 31);
+    if (__ldcg(&A.inlist[u >> 5]) & bit) return;
+    unsigned old = atomicOr(&A.inlist[u >> 5], bit);
+    if (old & bit) return;
+    uint32_t d = (uint32_t)(A.rowptr[u + 1] - A.rowptr[u]);
+    if (d > HX_WARP_MAX) {
+        unsigned long long p = atomicAdd(&A.ctl->big_len[nxt], 1ull);
+        A.big[nxt][p] = u;
+    } else {
+        unsigned long long p = atomicAdd(&A.ctl->list_len[nxt], 1ull);
+        A.list[nxt][p] = u;
+    }
+}
+
+// One warp: recompute vertex v (row length <= HX_WARP_MAX).  hist: this warp's
+// HX_WARP_MAX+1 shared bins.  Returns true if c[v] dropped.
+__device__ bool hx_warp_vertex(const HxArgs &A, uint32_t v, unsigned nxt, uint32_t *hist, unsigned lane) {
+    const int64_t s = A.rowptr[v], e = A.rowptr[v + 1];
+    const uint32_t cap = __ldcg(&A.c[v]);
+    if (cap == 0) return false;
+    uint32_t cnt = 0;
+    for (int64_t j = s + lane; j < e; j += 32) cnt += __ldcg(&A.c[A.col[j]]) >= cap ? 1u : 0u;
+    cnt = __reduce_add_sync(KC_FULL_MASK, cnt);
+    if (cnt >= cap) return false;  // support intact: estimate stands
+    // histogram of min(c[u], cap) over bins [0, cap]; cap <= degree <= HX_WARP_MAX
+    for (uint32_t b = lane; b <= cap; b += 32) hist[b] = 0;
+    __syncwarp();
+    for (int64_t j = s + lane; j < e; j += 32) {
+        uint32_t x = __ldcg(&A.c[A.col[j]]);
+        atomicAdd(&hist[x < cap ? x : cap], 1u);
+    }
+    __syncwarp();
+    // suffix scan from the top bin: largest k with sum_{x>=k} hist[x] >= k
+    uint32_t carry = 0, h = 0;
+    for (int64_t top = (int64_t)cap; top >= 1; top -= 32) {
+        int64_t k = top - lane;
+        uint32_t x = k >= 1 ? hist[k] : 0u;
+        uint32_t incl = x;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            uint32_t y = __shfl_up_sync(KC_FULL_MASK, incl, d);
+            if (lane >= (unsigned)d) incl += y;
+        }
+        bool ok = k >= 1 && carry + incl >= (uint32_t)k;
+        unsigned b = __ballot_sync(KC_FULL_MASK, ok);
+        if (b) {
+            h = (uint32_t)(top - (__ffs(b) - 1));
+            break;
+        }
+        carry += __shfl_sync(KC_FULL_MASK, incl, 31);
+    }
+    __syncwarp();
+    if (h >= cap) return false;
+    if (lane == 0) A.c[v] = h;
+    __syncwarp();
+    // neighbours whose estimate exceeds h may lose support
+    for (int64_t j = s + lane; j < e; j += 32) {
+        uint32_t u = A.col[j];
+        if (__ldcg(&A.c[u]) > h) hx_activate(A, u, nxt);
+    }
+    return true;
+}
+
+// Block-wide helpers for the CTA path.
+__device__ __forceinline__ uint32_t block_sum(uint32_t x, uint32_t *red) {
+    x = __reduce_add_sync(KC_FULL_MASK, x);
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) red[warp] = x;
+    __syncthreads();
+    uint32_t t = 0;
+    for (int w = 0; w < HX_WARPS; w++) t += red[w];
+    __syncthreads();
+    return t;
+}
+
+// Bins b in [0, nb) cover values [base + b*w, base + (b+1)*w); `above` counts
+// values beyond the last bin.  Returns the highest b whose suffix count
+// above + sum_{b' >= b} hist[b'] reaches base + b*w (the h-index lies in that
+// bin), or -1 if none does.
+__device__ int hx_block_suffix_find(const uint32_t *hist, int nb, uint64_t base, uint64_t w, uint64_t above,
+                                    uint32_t *red) {
+    // each thread owns HX_BINS / HX_THREADS consecutive bins
+    constexpr int PER = HX_BINS / HX_THREADS;
+    const int t = threadIdx.x;
+    // suffix sums: thread t covers bins [t*PER, t*PER+PER); we need, for each
+    // bin, the count of bins above it -> scan in reverse thread order
+    uint32_t local[PER];
+    uint32_t sum = 0;
+#pragma unroll
+    for (int i = PER - 1; i >= 0; i--) {
+        int b = t * PER + i;
+        local[i] = b < nb ? hist[b] : 0u;
+        sum += local[i];
+    }
+    // exclusive scan over threads in reverse order (threads above t)
+    const unsigned lane = t & 31, warp = t >> 5;
+    uint32_t v = sum;
+    // reverse within warp: use shfl_down to accumulate lanes above
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        uint32_t y = __shfl_down_sync(KC_FULL_MASK, v, d);
+        if (lane + d < 32) v += y;
+    }
+    // v = inclusive suffix within warp (this lane and above)
+    __shared__ uint32_t wsum[HX_WARPS];
+    __shared__ int best;
+    if (lane == 0) wsum[warp] = v;
+    if (t == 0) best = -1;
+    __syncthreads();
+    uint32_t warps_above = 0;
+    for (int w2 = warp + 1; w2 < HX_WARPS; w2++) warps_above += wsum[w2];
+    uint64_t suffix = (uint64_t)(v - sum) + warps_above + above;  // bins above this thread's range
+    int mybest = -1;
+#pragma unroll
+    for (int i = PER - 1; i >= 0; i--) {
+        int b = t * PER + i;
+        suffix += local[i];
+        if (b < nb && suffix >= base + (uint64_t)b * w && mybest < 0) mybest = b;
+    }
+    if (mybest >= 0) atomicMax(&best, mybest);
+    __syncthreads();
+    int r = best;
+    __syncthreads();
+    (void)red;
+    return r;
+}
+
+// One CTA: recompute vertex v with a long row.
+__device__ bool hx_block_vertex(const HxArgs &A, uint32_t v, unsigned nxt, uint32_t *hist, uint32_t *red) {
+    const int64_t s = A.rowptr[v], e = A.rowptr[v + 1];
+    __shared__ uint32_t cap_sh;
+    if (threadIdx.x == 0) cap_sh = __ldcg(&A.c[v]);
+    __syncthreads();
+    const uint32_t cap = cap_sh;
+    if (cap == 0) return false;
+    uint32_t cnt = 0;
+    for (int64_t j = s + threadIdx.x; j < e; j += HX_THREADS) cnt += __ldcg(&A.c[A.col[j]]) >= cap ? 1u : 0u;
+    cnt = block_sum(cnt, red);
+    if (cnt >= cap) return false;
+    // narrow [lo, hi) -- known to contain h -- with 4096-bin passes until the
+    // bins are one value wide; `above` counts neighbours at >= hi
+    uint64_t lo = 0, hi = cap;
+    uint32_t h = 0;
+    for (;;) {
+        const uint64_t w = (hi - lo + HX_BINS - 1) / HX_BINS;
+        const int nb = (int)((hi - lo + w - 1) / w);
+        for (int b = threadIdx.x; b < (int)HX_BINS; b += HX_THREADS) hist[b] = 0;
+        __syncthreads();
+        uint32_t above = 0;
+        for (int64_t j = s + threadIdx.x; j < e; j += HX_THREADS) {
+            uint32_t x = __ldcg(&A.c[A.col[j]]);
+            if (x >= hi) above++;
+            else if (x >= lo) atomicAdd(&hist[(x - lo) / w], 1u);
+        }
+        above = block_sum(above, red);
+        int b = hx_block_suffix_find(hist, nb, lo, w, above, red);
+        if (b < 0) b = 0;  // count(>= lo) >= lo holds by construction
+        if (w == 1) {
+            h = (uint32_t)(lo + b);
+            break;
+        }
+        const uint64_t nlo = lo + (uint64_t)b * w;
+        hi = nlo + w < hi ? nlo + w : hi;
+        lo = nlo;
+    }
+    if (h >= cap) return false;
+    if (threadIdx.x == 0) A.c[v] = h;
+    __syncthreads();
+    for (int64_t j = s + threadIdx.x; j < e; j += HX_THREADS) {
+        uint32_t u = A.col[j];
+        if (__ldcg(&A.c[u]) > h) hx_activate(A, u, nxt);
+    }
+    __syncthreads();
+    return true;
+}
+
+constexpr uint32_t HX_SMEM_WORDS =
+    HX_WARPS * (HX_WARP_MAX + 1) > HX_BINS ? HX_WARPS * (HX_WARP_MAX + 1) : HX_BINS;
+
+__global__ void __launch_bounds__(HX_THREADS, 2) hindex_kernel(HxArgs A) {
+    __shared__ uint32_t hist[HX_SMEM_WORDS];
+    __shared__ uint32_t red[HX_WARPS];
+    __shared__ unsigned int changed_sh;
+    __shared__ unsigned long long item_sh;
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    HindexCtl *ctl = A.ctl;
+    const unsigned G = gridDim.x;
+    for (uint32_t sweep = 0;; sweep++) {
+        const unsigned cur = sweep & 1, nxt = cur ^ 1;
+        if (threadIdx.x == 0) changed_sh = 0;
+        __syncthreads();
+        // high-degree vertices: one CTA each, taken dynamically
+        const unsigned long long nbig = ld_relaxed64(&ctl->big_len[cur]);
+        for (;;) {
+            if (threadIdx.x == 0) item_sh = atomicAdd(&ctl->big_cursor, 1ull);
+            __syncthreads();
+            unsigned long long i = item_sh;
+            __syncthreads();
+            if (i >= nbig) break;
+            uint32_t v = A.big[cur][i];
+            if (sweep > 0 && threadIdx.x == 0) atomicAnd(&A.inlist[v >> 5], ~(1u << (v & 31)));
+            __syncthreads();
+            if (hx_block_vertex(A, v, nxt, hist, red) && threadIdx.x == 0) changed_sh = 1;
+            __syncthreads();
+        }
+        // the rest: one warp per vertex; sweep 0 covers every vertex
+        const unsigned long long nsmall = sweep == 0 ? (unsigned long long)A.n : ld_relaxed64(&ctl->list_len[cur]);
+        uint32_t *wh = hist + warp * (HX_WARP_MAX + 1);
+        bool wchanged = false;
+        for (unsigned long long i = (unsigned long long)blockIdx.x * HX_WARPS + warp; i < nsmall;
+             i += (unsigned long long)G * HX_WARPS) {
+            uint32_t v = sweep == 0 ? (uint32_t)i : A.list[cur][i];
+            if (sweep == 0) {
+                if (A.rowptr[v + 1] - A.rowptr[v] > (int64_t)HX_WARP_MAX) continue;
+            } else if (lane == 0) {
+                atomicAnd(&A.inlist[v >> 5], ~(1u << (v & 31)));
+            }
+            __syncwarp();
+            wchanged |= hx_warp_vertex(A, v, nxt, wh, lane);
+        }
+        if (lane == 0 && wchanged) changed_sh = 1;
+        __syncthreads();
+        if (threadIdx.x == 0 && changed_sh) atomicOr(&ctl->changed, 1u);
+        if (!grid_barrier(&ctl->bar_count, &ctl->bar_gen, G, &ctl->err, KC_ERR_TIMEOUT, A.timeout_ns)) return;
+        // one CTA resets the consumed lists; everyone reads the verdict after a second barrier
+        __shared__ unsigned int go_on;
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            ctl->list_len[cur] = 0;
+            ctl->big_len[cur] = 0;
+            ctl->big_cursor = 0;
+            ctl->sweeps = sweep + 1;
+            unsigned ch = ctl->changed;
+            ctl->changed = 0;
+            unsigned long long pend = ctl->list_len[nxt] + ctl->big_len[nxt];
+            ctl->cursor = (ch && pend > 0) ? 1ull : 0ull;  // reuse as the continue flag
+            if (sweep + 1 >= A.max_sweeps && pend > 0) atomicCAS(&ctl->err, 0u, (unsigned)KC_ERR_CAPACITY);
+            __threadfence();
+        }
+        if (!grid_barrier(&ctl->bar_count, &ctl->bar_gen, G, &ctl->err, KC_ERR_TIMEOUT, A.timeout_ns)) return;
+        // CTA 0 rewrites the flag only after the next sweep's first barrier,
+        // by which time every CTA has read it
+        if (threadIdx.x == 0) go_on = (unsigned)ld_relaxed64(&ctl->cursor);
+        __syncthreads();
+        if (!go_on) return;
+    }
+}
+
+static int ensure_hx_buffers(Graph *g) {
+    const uint64_t n = g->n;
+    if (!g->core) KC_TRY(dalloc(&g->core, n + 1, "core"));
+    if (!g->bitmap) KC_TRY(dalloc(&g->bitmap, (n + 31) / 32 + 1, "active bitmap"));
+    for (int i = 0; i < 2; i++) {
+        if (!g->list[i]) KC_TRY(dalloc(&g->list[i], n + 1, "active list"));
+        if (!g->big[i]) KC_TRY(dalloc(&g->big[i], n + 1, "active list (long rows)"));
+    }
+    if (!g->hctl) KC_TRY(dalloc(&g->hctl, 1, "h-index control"));
+    return KC_OK;
+}
+
+int hindex_run(Graph *g, cudaStream_t s, kc_stats *st) {
+    KC_TRY(ensure_hx_buffers(g));
+    int coop = 0;
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, g->device);
+    if (!coop) return fail(KC_ERR_UNSUPPORTED, "device lacks cooperative launch");
+    int occ = 0;
+    KC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, hindex_kernel, HX_THREADS, 0));
+    if (occ < 1) return fail(KC_ERR_UNSUPPORTED, "h-index kernel cannot be resident");
+    const int grid = occ * g->sm_count;
+    if (!g->ev0) {
+        KC_CUDA(cudaEventCreate(&g->ev0));
+        KC_CUDA(cudaEventCreate(&g->ev1));
+        KC_CUDA(cudaEventCreate(&g->evk0));
+        KC_CUDA(cudaEventCreate(&g->evk1));
+    }
+    HxArgs A;
+    A.rowptr = g->rowptr;
+    A.col = g->col;
+    A.n = g->n;
+    A.c = g->core;
+    A.inlist = g->bitmap;
+    A.list[0] = g->list[0];
+    A.list[1] = g->list[1];
+    A.big[0] = g->big[0];
+    A.big[1] = g->big[1];
+    A.ctl = g->hctl;
+    A.timeout_ns = 20ull * 1000 * 1000 * 1000;
+    A.max_sweeps = g->n + 3;  // a path needs O(n) sweeps
+    KC_CUDA(cudaEventRecord(g->ev0, s));
+    KC_CUDA(cudaMemsetAsync(g->hctl, 0, sizeof(HindexCtl), s));
+    const int ig = std::max(1, std::min<int>(g->sm_count * 8, (int)((g->n + 255) / 256)));
+    hindex_init<<<ig, 256, 0, s>>>(g->rowptr, g->n, g->core, g->bitmap, g->big[0], g->hctl);
+    void *args[] = {&A};
+    KC_CUDA(cudaEventRecord(g->evk0, s));
+    KC_CUDA(cudaLaunchCooperativeKernel((const void *)hindex_kernel, dim3(grid), dim3(HX_THREADS), args, 0, s));
+    KC_CUDA(cudaEventRecord(g->evk1, s));
+    KC_CUDA(cudaEventRecord(g->ev1, s));
+    HindexCtl h;
+    KC_CUDA(cudaMemcpyAsync(&h, g->hctl, sizeof(h), cudaMemcpyDeviceToHost, s));
+    KC_CUDA(cudaStreamSynchronize(s));
+    float ms = 0.f, kms = 0.f;
+    cudaEventElapsedTime(&ms, g->ev0, g->ev1);
+    cudaEventElapsedTime(&kms, g->evk0, g->evk1);
+    g->last_ms = ms;
+    g->last_kernel_ms = kms;
+    if (h.err) {
+        g->core_valid = false;
+        return fail((int)h.err, "h-index kernel raised error %u", h.err);
+    }
+    g->core_valid = true;
+    if (st) {
+        st->iterations = h.sweeps;
+        st->levels = 0;
+        st->ms = ms;
+    }
+    return KC_OK;
+}
+
+}  // namespace kc

@@ -1,0 +1,130 @@
+// Internal declarations shared by the translation units of libkcore.so.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+
+#include "../../include/kcore.h"
+
+namespace kc {
+
+// Records a formatted message for kc_last_error() and returns `code`.
+int fail(int code, const char *fmt, ...);
+void clear_error();
+
+#define KC_CUDA(call)                                                                          \
+    do {                                                                                       \
+        cudaError_t e_ = (call);                                                               \
+        if (e_ != cudaSuccess)                                                                 \
+            return ::kc::fail(KC_ERR_CUDA, "%s:%d %s: %s", __FILE__, __LINE__, #call,          \
+                              cudaGetErrorString(e_));                                         \
+    } while (0)
+
+#define KC_TRY(expr)                 \
+    do {                             \
+        int rc_ = (expr);            \
+        if (rc_ != KC_OK) return rc_; \
+    } while (0)
+
+// Device allocation helpers: report KC_ERR_NOMEM with the size on failure.
+int dmalloc(void **p, size_t bytes, const char *what);
+void dfree(void *p);
+
+template <class T>
+int dalloc(T **p, size_t count, const char *what) {
+    return dmalloc(reinterpret_cast<void **>(p), count * sizeof(T) + 16, what);
+}
+
+// Control block of the persistent bucket peel (one per graph, device memory).
+// Slots [i % 3] belong to level index i; see peel.cu.
+struct PeelCtl {
+    unsigned long long pending[3];   // outstanding work credits of level i
+    unsigned int next_min[3];        // smallest residual degree above level i
+    unsigned int nonempty[3];        // some vertex was claimed at level i
+    unsigned long long gq_head;      // global spill queue, consumer index
+    unsigned long long gq_tail;      // global spill queue, producer index
+    unsigned int err;                // KC_ERR_* raised on the device
+    unsigned int err_info;           // where it was raised
+    unsigned int level_indices;      // level indices processed
+    unsigned int levels;             // non-empty levels
+    unsigned int kmax;               // largest level with a claim
+    unsigned int pad;
+};
+
+// Control block of the h-index iteration.
+struct HindexCtl {
+    unsigned long long list_len[2];  // active list lengths (ping-pong)
+    unsigned long long big_len[2];   // high-degree active list lengths
+    unsigned long long cursor;       // work cursor (small items)
+    unsigned long long big_cursor;   // work cursor (high-degree items)
+    unsigned int bar_count;          // grid barrier arrivals
+    unsigned int bar_gen;            // grid barrier generation
+    unsigned int sweeps;
+    unsigned int changed;
+    unsigned int err;
+    unsigned int err_info;
+};
+
+struct Graph {
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t stream = nullptr;
+    uint32_t n = 0;
+    uint64_t nnz = 0;
+    uint32_t max_deg = 0;
+    uint64_t num_vnodes = 0;
+    double build_ms = 0.0;
+
+    int64_t *rowptr = nullptr;  // [n+1]
+    uint32_t *col = nullptr;    // [nnz]
+    uint32_t *core = nullptr;   // [n]  residual degree / estimate -> core numbers
+    bool core_valid = false;
+
+    // decomposition work buffers (allocated on first use, kept for reuse)
+    uint32_t *bitmap = nullptr;       // [ceil(n/32)]  claimed / active flags
+    uint32_t *alive = nullptr;        // [n]           per-CTA alive segments
+    unsigned long long *gq = nullptr; // spill queue of work items (sentinel = ~0)
+    unsigned long long gq_cap = 0;
+    bool gq_clean = false;            // gq holds only sentinels
+    PeelCtl *peel_ctl = nullptr;
+    uint32_t *list[2] = {nullptr, nullptr};  // h-index active lists
+    uint32_t *big[2] = {nullptr, nullptr};   // h-index high-degree lists
+    HindexCtl *hctl = nullptr;
+    uint32_t *red = nullptr;          // small reduction scratch (min/max)
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, evk0 = nullptr, evk1 = nullptr;
+    double last_ms = 0.0, last_kernel_ms = 0.0;
+
+    ~Graph();
+};
+
+// csr_build.cu
+int build_csr_from_edges(Graph *g, const uint32_t *d_src, const uint32_t *d_dst, uint64_t m, uint32_t n,
+                         uint32_t flags);
+int exclusive_scan_u32_i64(const uint32_t *d_in, int64_t *d_out, uint64_t n, cudaStream_t s);
+int graph_finish(Graph *g);  // max degree, vnode count
+int graph_validate(Graph *g, uint64_t *bad);
+int virtual_layout(Graph *g, uint32_t part_size, uint32_t *h_node_pointer, uint32_t *h_edge_list,
+                   uint32_t *h_parts, uint64_t *num_parts);
+
+// peel.cu
+int peel_run(Graph *g, cudaStream_t s, bool gpp_zero_to_one, kc_stats *st);
+// hindex.cu
+int hindex_run(Graph *g, cudaStream_t s, kc_stats *st);
+
+// mtx_loader.cpp
+int parse_mtx(const char *path, int mode, uint32_t *n, uint64_t *m, uint32_t **src, uint32_t **dst);
+
+// gen.cu
+int gen_rmat(uint32_t scale, uint64_t num_edges, double a, double b, double c, uint64_t seed,
+             uint32_t *d_src, uint32_t *d_dst, cudaStream_t s);
+int gen_er(uint32_t n, uint64_t m, uint64_t seed, uint32_t *d_src, uint32_t *d_dst, cudaStream_t s);
+int gen_planted(uint32_t n, uint32_t k, double p, uint64_t seed, uint32_t *d_src, uint32_t *d_dst,
+                uint64_t cap, uint64_t *m, cudaStream_t s);
+
+}  // namespace kc
+
+struct kc_graph : kc::Graph {};

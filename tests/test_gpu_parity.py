@@ -1,0 +1,210 @@
+"""Parity of the CUDA engine with the oracle (bit-exact integer results),
+through the C ABI.  Runs on the GB300."""
+import numpy as np
+import pytest
+
+from oracle import gen as gen_ref
+import oracle
+import pico_gb300 as pg
+
+pytestmark = pytest.mark.gpu
+
+ALL = ["HistoCore", "CntCore", "NbrCore", "peelone", "gppeel", "peelone_dyn", "peel_dyn"]
+CASES = ["example", "zero_based_dups", "dups_selfloops", "sparse_ids", "hub150", "er300", "rmat9",
+         "clique40_path", "no_edges", "only_selfloops"]
+
+
+def expected(method, core, rowptr):
+    """The reference's output for `method` given the true core numbers."""
+    if method == "gppeel":
+        return np.where(np.diff(rowptr) == 0, 1, core).astype(np.uint32)
+    return core
+
+
+def check_all_methods(g, rowptr, col, methods=ALL):
+    core, kmax = oracle.bz(rowptr, col)
+    for m in methods:
+        got, st = g.decompose(m)
+        exp = expected(m, core, rowptr)
+        assert got.shape == exp.shape
+        bad = np.flatnonzero(got != exp)
+        assert bad.size == 0, "%s: %d mismatches, first v=%d got %d want %d" % (
+            m, bad.size, bad[0], got[bad[0]], exp[bad[0]])
+        if g.n:
+            assert st.kmax == int(exp.max())
+            assert st.kmin == min(10, int(exp.min()))
+    return core
+
+
+def test_example_known_answer(golden, mtx_file):
+    path = mtx_file(golden["example"]["text"])
+    for mode in ("coo", "csr"):
+        g = pg.Graph.from_mtx(path, mode)
+        for m in ALL:
+            core, st = g.decompose(m)
+            assert core.tolist() == [2, 2, 2, 2, 2]
+            assert st.kmax == 2 and st.kmin == 2
+        g.free()
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_golden_inputs_all_methods(golden, mtx_file, name):
+    case = golden[name]
+    path = mtx_file(case["text"])
+    g = pg.Graph.from_mtx(path, "coo")
+    coo = case["coo"]
+    assert g.n == coo["n"] and g.nnz == 2 * coo["m"]
+    rp, col = g.csr()
+    core = check_all_methods(g, rp, col)
+    assert core.tolist() == case["core_bz_coo"]
+    if g.n:
+        # the reference's virtual-graph layout, built on the device
+        node_ptr, edge_list, parts = g.virtual_layout(64)
+        assert node_ptr.tolist() == coo["node_pointer"]
+        assert edge_list.tolist() == coo["edge_list"]
+        assert parts.tolist() == coo["parts"]
+    g.free()
+    if "csr" in case:
+        g = pg.Graph.from_mtx(path, "csr")
+        rp, col = g.csr()
+        assert g.n == case["csr"]["V"]
+        assert rp.tolist() == case["csr"]["offsets"] and col.tolist() == case["csr"]["neighbors"]
+        core = check_all_methods(g, rp, col)
+        assert core.tolist() == case["core_bz_csr"]
+        g.free()
+
+
+def random_edges(rng, n, m):
+    return rng.integers(0, n, size=m).astype(np.uint32), rng.integers(0, n, size=m).astype(np.uint32)
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_random_graphs_all_methods(seed):
+    rng = np.random.default_rng(100 + seed)
+    n = int(rng.integers(50, 20000))
+    m = int(rng.integers(n, 20 * n))
+    s, d = random_edges(rng, n, m)
+    g = pg.Graph.from_edges(s, d, n, dedup=True)
+    rp, col = g.csr()
+    erp, ecol = oracle.csr_dedup(n, s, d)
+    assert np.array_equal(rp, erp) and np.array_equal(col, ecol)
+    check_all_methods(g, rp, col)
+    assert g.validate() == 0
+
+
+def test_multigraph_keeps_parallel_edges_in_edge_order():
+    rng = np.random.default_rng(5)
+    n, m = 3000, 40000
+    s, d = random_edges(rng, 300, m)  # many repeats
+    g = pg.Graph.from_edges(s, d, n)
+    rp, col = g.csr()
+    erp, ecol = oracle.csr_multi(n, s, d)
+    assert np.array_equal(rp, erp) and np.array_equal(col, ecol)
+    check_all_methods(g, rp, col)
+
+
+def test_sort_rows_without_dedup():
+    rng = np.random.default_rng(6)
+    s, d = random_edges(rng, 500, 20000)
+    g = pg.Graph.from_edges(s, d, 500, sort_rows=True)
+    rp, col = g.csr()
+    erp, ecol = oracle.csr_multi(500, s, d)
+    assert np.array_equal(rp, erp)
+    for v in range(500):
+        assert np.array_equal(col[rp[v]:rp[v + 1]], np.sort(ecol[erp[v]:erp[v + 1]]))
+
+
+def test_structured_graphs():
+    # star (one hub above the chunk size), long path (deep cascade within a
+    # level), clique, disjoint union with isolated ids
+    cases = []
+    hub = 50000
+    cases.append((hub + 1, np.zeros(hub, np.uint32), np.arange(1, hub + 1, dtype=np.uint32)))
+    L = 200000
+    cases.append((L, np.arange(L - 1, dtype=np.uint32), np.arange(1, L, dtype=np.uint32)))
+    k = 300
+    a, b = np.triu_indices(k, 1)
+    cases.append((k, a.astype(np.uint32), b.astype(np.uint32)))
+    s = np.concatenate([a, a + 1000, [5000]]).astype(np.uint32)
+    d = np.concatenate([b, b + 1000, [5001]]).astype(np.uint32)
+    cases.append((6000, s, d))
+    for n, s, d in cases:
+        g = pg.Graph.from_edges(s, d, n, dedup=True)
+        rp, col = g.csr()
+        check_all_methods(g, rp, col)
+        g.free()
+
+
+def test_hub_rows_large_sort_and_stable_order():
+    # rows far above 4096 entries take the radix path of the row sort
+    rng = np.random.default_rng(9)
+    n = 70000
+    s = np.concatenate([np.zeros(60000), rng.integers(0, n, 30000)]).astype(np.uint32)
+    d = np.concatenate([rng.integers(1, n, 60000), rng.integers(0, n, 30000)]).astype(np.uint32)
+    g = pg.Graph.from_edges(s, d, n, dedup=True)
+    rp, col = g.csr()
+    erp, ecol = oracle.csr_dedup(n, s, d)
+    assert np.array_equal(rp, erp) and np.array_equal(col, ecol)
+    g2 = pg.Graph.from_edges(s, d, n)
+    rp2, col2 = g2.csr()
+    erp2, ecol2 = oracle.csr_multi(n, s, d)
+    assert np.array_equal(rp2, erp2) and np.array_equal(col2, ecol2)
+    check_all_methods(g, rp, col, ["peelone_dyn", "NbrCore"])
+
+
+def test_generators_match_host_restatement():
+    s, d, m = pg.gen_rmat_edges(12, 20000, seed=42)
+    es, ed = gen_ref.rmat(12, 20000, 42)
+    assert np.array_equal(s.download(np.uint32, m), es) and np.array_equal(d.download(np.uint32, m), ed)
+    s, d, m = pg.gen_er_edges(1000, 30000, seed=7)
+    es, ed = gen_ref.er(1000, 30000, 7)
+    gs, gd = s.download(np.uint32, m), d.download(np.uint32, m)
+    assert np.array_equal(gs, es) and np.array_equal(gd, ed)
+    assert (gs < gd).all() and np.unique(gs.astype(np.int64) * 1000 + gd).size == m  # without replacement
+    s, d, m = pg.gen_planted_edges(100000, 60, 0.6, seed=3)
+    es, ed = gen_ref.planted(100000, 60, 0.6, 3)
+    assert m == es.size
+    assert np.array_equal(s.download(np.uint32, m), es) and np.array_equal(d.download(np.uint32, m), ed)
+
+
+def test_repeated_decompositions_and_device_output():
+    g = pg.rmat_graph(14, 8, seed=1)
+    rp, col = g.csr()
+    core, _ = oracle.bz(rp, col)
+    for _ in range(3):
+        for m in ("peelone_dyn", "NbrCore", "gppeel"):
+            got, _ = g.decompose(m)
+            assert np.array_equal(got, expected(m, core, rp))
+    g.decompose_device("peel_dyn")
+    buf = pg.DeviceBuffer(4 * g.n)
+    pg.check(pg.lib().kc_memcpy(pg.ctypes.c_void_p(buf.ptr), pg.ctypes.c_void_p(g.device_core()), 4 * g.n, 3))
+    assert np.array_equal(buf.download(np.uint32, g.n), core)
+
+
+def test_invalid_inputs_fail_with_status():
+    with pytest.raises(pg.KCoreError) as e:
+        pg.Graph.from_edges([0, 5], [1, 2], 3)
+    assert e.value.code == pg.KC_ERR_INVALID
+    g = pg.Graph.from_edges([0], [1], 2)
+    with pytest.raises(pg.KCoreError) as e:
+        pg.check(pg.lib().kc_decompose(g.handle, 99, None, 0, None, None))
+    assert e.value.code == pg.KC_ERR_INVALID
+
+
+def test_config1_er_65536_1m():
+    g = pg.er_graph(65536, 1048576, seed=1)
+    assert g.n == 65536 and g.nnz == 2 * 1048576
+    rp, col = g.csr()
+    check_all_methods(g, rp, col, ["peelone_dyn", "NbrCore", "HistoCore", "gppeel"])
+    assert g.validate() == 0
+
+
+def test_config2_rmat22_ef16():
+    g = pg.rmat_graph(22, 16, seed=2)
+    rp, col = g.csr()
+    assert g.n == 1 << 22 and g.validate() == 0
+    core, kmax = oracle.bz(rp, col)
+    for m in ("peelone_dyn", "NbrCore"):
+        got, st = g.decompose(m)
+        assert np.array_equal(got, core), m
+        assert st.kmax == kmax
