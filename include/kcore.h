@@ -171,6 +171,27 @@ int kc_decompose(kc_graph *g, int method, uint32_t *core_out, int out_on_device,
  * covers every kernel of the call (initialisation included), *kernel_ms the
  * main decomposition kernel alone.  Either pointer may be NULL. */
 int kc_graph_last_timing(const kc_graph *g, double *total_ms, double *kernel_ms);
+/* Tunables of the decomposition kernels, set per graph (the autotuner and
+ * the benchmarks use these).  Names: "peel.chunk" (row entries per peel work
+ * item), "peel.spill" (cascade items a CTA keeps before publishing to the
+ * shared queues), "peel.steal" (items taken per steal), "peel.queues" (number
+ * of shared queues, 1..64), "peel.ctas_per_sm" (0 = occupancy maximum),
+ * "trace" (1 = record a per-level trace of the next decompositions). */
+int kc_graph_set_param(kc_graph *g, const char *name, int64_t value);
+
+/* Per-level trace of the last peel decomposition (recorded when the "trace"
+ * parameter is 1): one record per level index. */
+typedef struct kc_level_trace {
+    uint64_t t_start_ns;  /* GPU global timer when the level began (CTA 0) */
+    uint32_t level;       /* level value L */
+    uint32_t claimed;     /* vertices peeled at this level */
+    uint32_t scan_len;    /* alive-list length scanned */
+    uint32_t spilled;     /* items published on the shared queues */
+    uint32_t steals;      /* successful steals */
+    uint32_t steal_fail;  /* failed steal attempts */
+} kc_level_trace;
+int kc_graph_trace(const kc_graph *g, kc_level_trace *out, uint32_t cap, uint32_t *count);
+
 /* Device pointer of the last decomposition's core array (n uint32). */
 int kc_graph_device_core(const kc_graph *g, const uint32_t **d_core);
 

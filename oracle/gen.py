@@ -20,6 +20,24 @@ def _thr(p):
 
 
 def rmat(scale, m, seed, a=0.57, b=0.19, c=0.19):
+    """R-MAT edge list (src, dst); the C restatement for large m."""
+    if m > 1 << 20:
+        import ctypes
+        import oracle
+        L = oracle.lib()
+        u32p = ctypes.POINTER(ctypes.c_uint32)
+        L.orc_gen_rmat.argtypes = [ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64,
+                                   ctypes.c_uint64, ctypes.c_uint64, u32p, u32p]
+        L.orc_gen_rmat.restype = None
+        src = np.empty(m, dtype=np.uint32)
+        dst = np.empty(m, dtype=np.uint32)
+        L.orc_gen_rmat(scale, m, _thr(a), _thr(a + b), _thr(a + b + c), seed,
+                       src.ctypes.data_as(u32p), dst.ctypes.data_as(u32p))
+        return src, dst
+    return rmat_numpy(scale, m, seed, a, b, c)
+
+
+def rmat_numpy(scale, m, seed, a=0.57, b=0.19, c=0.19):
     i = np.arange(m, dtype=np.uint64)
     with np.errstate(over="ignore"):
         base = mix64(np.uint64(seed) * np.uint64(0xD1B54A32D192ED03) + i)

@@ -313,37 +313,74 @@ int orc_make_ugraph(uint32_t n, uint64_t m, const uint32_t *src, const uint32_t 
 }
 
 /* ------------------------------------------------------------------------ */
-static int cmp_u64(const void *a, const void *b)
+static int cmp_u32(const void *a, const void *b)
 {
-    uint64_t x = *(const uint64_t *)a, y = *(const uint64_t *)b;
+    uint32_t x = *(const uint32_t *)a, y = *(const uint32_t *)b;
     return (x > y) - (x < y);
+}
+
+/* In-place LSD radix sort of a short array through `tmp` (same length). */
+static void radix_u32(uint32_t *a, uint32_t *tmp, uint64_t len)
+{
+    uint64_t cnt[256];
+    uint32_t *src = a, *dst = tmp;
+    for (int shift = 0; shift < 32; shift += 8) {
+        memset(cnt, 0, sizeof(cnt));
+        for (uint64_t i = 0; i < len; i++) cnt[(src[i] >> shift) & 255u]++;
+        uint64_t s = 0;
+        for (int d = 0; d < 256; d++) { uint64_t c = cnt[d]; cnt[d] = s; s += c; }
+        for (uint64_t i = 0; i < len; i++) dst[cnt[(src[i] >> shift) & 255u]++] = src[i];
+        uint32_t *t = src; src = dst; dst = t;
+    }
 }
 
 /* De-duplicated, sorted CSR of peel/src/graph.cpp:103-131 (a std::set per
  * vertex): both directions of every non-self-loop edge, each neighbour once,
  * ascending.  rowptr must hold n+1 entries; col must hold 2*m entries.
+ * Counting sort by row, then each row sorted and made unique.
  * Returns the number of CSR entries, or -1 on allocation failure.         */
 int64_t orc_csr_dedup(uint32_t n, uint64_t m, const uint32_t *src, const uint32_t *dst,
                       int64_t *rowptr, uint32_t *col)
 {
-    uint64_t *key = (uint64_t *)malloc((size_t)(2 * m + 1) * sizeof(uint64_t));
-    if (!key) return -1;
-    uint64_t k = 0;
+    int64_t *start = (int64_t *)calloc((size_t)n + 2, sizeof(int64_t));
+    uint32_t *tmp = NULL;
+    if (!start) return -1;
     for (uint64_t i = 0; i < m; i++) {
         if (src[i] == dst[i]) continue;
-        key[k++] = ((uint64_t)src[i] << 32) | dst[i];
-        key[k++] = ((uint64_t)dst[i] << 32) | src[i];
+        start[src[i] + 1]++;
+        start[dst[i] + 1]++;
     }
-    qsort(key, (size_t)k, sizeof(uint64_t), cmp_u64);
-    for (uint32_t v = 0; v <= n; v++) rowptr[v] = 0;
+    for (uint32_t v = 0; v < n; v++) start[v + 1] += start[v];
+    int64_t total = start[n];
+    int64_t *fill = (int64_t *)malloc(((size_t)n + 1) * sizeof(int64_t));
+    if (!fill) { free(start); return -1; }
+    memcpy(fill, start, ((size_t)n + 1) * sizeof(int64_t));
+    for (uint64_t i = 0; i < m; i++) {
+        if (src[i] == dst[i]) continue;
+        col[fill[src[i]]++] = dst[i];
+        col[fill[dst[i]]++] = src[i];
+    }
+    free(fill);
+    uint64_t maxlen = 0;
+    for (uint32_t v = 0; v < n; v++) {
+        uint64_t l = (uint64_t)(start[v + 1] - start[v]);
+        if (l > maxlen) maxlen = l;
+    }
+    if (maxlen > 256) tmp = (uint32_t *)malloc((size_t)maxlen * sizeof(uint32_t));
     int64_t w = 0;
-    for (uint64_t i = 0; i < k; i++) {
-        if (i > 0 && key[i] == key[i - 1]) continue;
-        rowptr[(key[i] >> 32) + 1]++;
-        col[w++] = (uint32_t)key[i];
+    rowptr[0] = 0;
+    for (uint32_t v = 0; v < n; v++) {
+        uint32_t *row = col + start[v];
+        uint64_t l = (uint64_t)(start[v + 1] - start[v]);
+        if (l > 256 && tmp) radix_u32(row, tmp, l);
+        else qsort(row, (size_t)l, sizeof(uint32_t), cmp_u32);
+        for (uint64_t j = 0; j < l; j++)
+            if (j == 0 || row[j] != row[j - 1]) col[w++] = row[j];
+        rowptr[v + 1] = w;
     }
-    for (uint32_t v = 0; v < n; v++) rowptr[v + 1] += rowptr[v];
-    free(key);
+    (void)total;
+    free(tmp);
+    free(start);
     return w;
 }
 
@@ -365,4 +402,35 @@ uint64_t orc_check_local(uint32_t n, const int64_t *rowptr, const uint32_t *col,
         if (ge < c[v] || gt > c[v]) bad++;
     }
     return bad;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Host restatement of the device R-MAT generator (pico_gb300/csrc/gen.cu):
+ * edge i draws its quadrants from the splitmix64 finaliser of a counter, so
+ * the same (scale, m, seed, thresholds) give the same edge list.            */
+static uint64_t orc_mix64(uint64_t z)
+{
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+void orc_gen_rmat(uint32_t scale, uint64_t m, uint64_t ta, uint64_t tab, uint64_t tabc, uint64_t seed,
+                  uint32_t *src, uint32_t *dst)
+{
+    for (uint64_t i = 0; i < m; i++) {
+        uint64_t base = orc_mix64(seed * 0xD1B54A32D192ED03ull + i);
+        uint32_t u = 0, v = 0;
+        uint64_t word = 0;
+        for (uint32_t b = 0; b < scale; b++) {
+            if ((b & 1) == 0) word = orc_mix64(base ^ ((uint64_t)((b >> 1) + 1) * 0xA24BAED4963EE407ull));
+            uint32_t r = (uint32_t)(word >> (32 * (b & 1)));
+            uint32_t q = r < ta ? 0u : (r < tab ? 1u : (r < tabc ? 2u : 3u));
+            u = (u << 1) | (q >> 1);
+            v = (v << 1) | (q & 1u);
+        }
+        src[i] = u;
+        dst[i] = v;
+    }
 }

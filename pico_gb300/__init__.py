@@ -52,6 +52,12 @@ class kc_stats(ctypes.Structure):
                 ("build_ms", ctypes.c_double)]
 
 
+class kc_level_trace(ctypes.Structure):
+    _fields_ = [("t_start_ns", ctypes.c_uint64), ("level", ctypes.c_uint32), ("claimed", ctypes.c_uint32),
+                ("scan_len", ctypes.c_uint32), ("spilled", ctypes.c_uint32), ("steals", ctypes.c_uint32),
+                ("steal_fail", ctypes.c_uint32)]
+
+
 @dataclass
 class Stats:
     method: str
@@ -108,6 +114,8 @@ def lib():
     _sig(L, "kc_decompose", i, [_P, i, _P, i, ctypes.POINTER(kc_stats), _P])
     _sig(L, "kc_graph_device_core", i, [_P, PP])
     _sig(L, "kc_graph_last_timing", i, [_P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)])
+    _sig(L, "kc_graph_set_param", i, [_P, ctypes.c_char_p, ctypes.c_int64])
+    _sig(L, "kc_graph_trace", i, [_P, ctypes.POINTER(kc_level_trace), u32, _U32P])
     _sig(L, "kc_host_alloc", i, [PP, ctypes.c_size_t])
     _sig(L, "kc_host_free", i, [_P])
     _sig(L, "kc_device_alloc", i, [PP, ctypes.c_size_t, i])
@@ -323,6 +331,18 @@ class Graph:
         a, b = ctypes.c_double(), ctypes.c_double()
         check(lib().kc_graph_last_timing(self._h, ctypes.byref(a), ctypes.byref(b)))
         return a.value, b.value
+
+    def set_param(self, name, value):
+        check(lib().kc_graph_set_param(self._h, name.encode(), int(value)))
+
+    def trace(self):
+        """Per-level trace of the last peel (after set_param("trace", 1))."""
+        cnt = ctypes.c_uint32()
+        check(lib().kc_graph_trace(self._h, None, 0, ctypes.byref(cnt)))
+        buf = (kc_level_trace * max(cnt.value, 1))()
+        check(lib().kc_graph_trace(self._h, buf, cnt.value, ctypes.byref(cnt)))
+        keys = [f[0] for f in kc_level_trace._fields_]
+        return [{k: getattr(buf[i], k) for k in keys} for i in range(cnt.value)]
 
     def device_core(self):
         p = ctypes.c_void_p()

@@ -56,6 +56,7 @@ Graph::~Graph() {
     }
     dfree(hctl);
     dfree(red);
+    dfree(trace);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
     if (evk0) cudaEventDestroy(evk0);
@@ -362,6 +363,47 @@ int kc_decompose(kc_graph *g, int method, uint32_t *core_out, int out_on_device,
         KC_CUDA(cudaMemcpyAsync(core_out, g->core, (uint64_t)g->n * 4,
                                 out_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
         KC_CUDA(cudaStreamSynchronize(s));
+    }
+    return KC_OK;
+}
+
+int kc_graph_set_param(kc_graph *g, const char *name, int64_t value) {
+    clear_error();
+    if (!g || !name) return fail(KC_ERR_INVALID, "null argument");
+    std::string k(name);
+    Tuning &t = g->tune;
+    if (k == "peel.chunk") {
+        if (value < 256 || value > (1 << 20) || (value & (value - 1))) return fail(KC_ERR_INVALID, "peel.chunk: power of two in [256, 2^20]");
+        t.peel_chunk = (int)value;
+    } else if (k == "peel.spill") {
+        if (value < 0 || value > 3072) return fail(KC_ERR_INVALID, "peel.spill: [0, 3072]");
+        t.peel_spill = (int)value;
+    } else if (k == "peel.steal") {
+        if (value < 1 || value > 2048) return fail(KC_ERR_INVALID, "peel.steal: [1, 2048]");
+        t.peel_steal = (int)value;
+    } else if (k == "peel.queues") {
+        if (value < 1 || value > PEEL_MAX_QUEUES) return fail(KC_ERR_INVALID, "peel.queues: [1, %d]", PEEL_MAX_QUEUES);
+        t.peel_queues = (int)value;
+    } else if (k == "peel.ctas_per_sm") {
+        if (value < 0 || value > 32) return fail(KC_ERR_INVALID, "peel.ctas_per_sm: [0, 32]");
+        t.peel_ctas_per_sm = (int)value;
+    } else if (k == "trace") {
+        t.trace = value ? 1 : 0;
+    } else {
+        return fail(KC_ERR_INVALID, "unknown parameter %s", name);
+    }
+    return KC_OK;
+}
+
+int kc_graph_trace(const kc_graph *g, kc_level_trace *out, uint32_t cap, uint32_t *count) {
+    clear_error();
+    if (!g || !count) return fail(KC_ERR_INVALID, "null argument");
+    static_assert(sizeof(kc_level_trace) == sizeof(PeelTrace), "trace layout");
+    uint32_t c = g->trace_count;
+    *count = c;
+    if (out && cap && c) {
+        KC_CUDA(cudaSetDevice(g->device));
+        KC_CUDA(cudaMemcpy(out, g->trace, sizeof(PeelTrace) * std::min(c, cap), cudaMemcpyDeviceToHost));
     }
     return KC_OK;
 }

@@ -41,18 +41,44 @@ int dalloc(T **p, size_t count, const char *what) {
 
 // Control block of the persistent bucket peel (one per graph, device memory).
 // Slots [i % 3] belong to level index i; see peel.cu.
+constexpr int PEEL_MAX_QUEUES = 64;
+
+// One shared work queue: producer and consumer index on separate lines.
+struct alignas(128) PeelQueue {
+    unsigned long long head;
+    unsigned long long pad0[15];
+    unsigned long long tail;
+    unsigned long long pad1[15];
+};
+
 struct PeelCtl {
     unsigned long long pending[3];   // outstanding work credits of level i
+    unsigned long long scan_cursor[3];  // next alive-list tile of level i
+    unsigned long long out_len[3];   // survivors appended by level i's scan
     unsigned int next_min[3];        // smallest residual degree above level i
     unsigned int nonempty[3];        // some vertex was claimed at level i
-    unsigned long long gq_head;      // global spill queue, consumer index
-    unsigned long long gq_tail;      // global spill queue, producer index
     unsigned int err;                // KC_ERR_* raised on the device
     unsigned int err_info;           // where it was raised
     unsigned int level_indices;      // level indices processed
     unsigned int levels;             // non-empty levels
     unsigned int kmax;               // largest level with a claim
     unsigned int pad;
+    PeelQueue q[3][PEEL_MAX_QUEUES]; // shared spill queues of level i (slot i % 3)
+};
+
+// Per-level trace record (layout of kc_level_trace).
+struct PeelTrace {
+    unsigned long long t_start_ns;
+    unsigned int level, claimed, scan_len, spilled, steals, steal_fail;
+};
+
+struct Tuning {
+    int peel_chunk = 512;
+    int peel_spill = 32;
+    int peel_steal = 64;
+    int peel_queues = 16;
+    int peel_ctas_per_sm = 0;
+    int trace = 0;
 };
 
 // Control block of the h-index iteration.
@@ -86,9 +112,13 @@ struct Graph {
 
     // decomposition work buffers (allocated on first use, kept for reuse)
     uint32_t *bitmap = nullptr;       // [ceil(n/32)]  claimed / active flags
-    uint32_t *alive = nullptr;        // [n]           per-CTA alive segments
-    unsigned long long *gq = nullptr; // spill queue of work items (sentinel = ~0)
-    unsigned long long gq_cap = 0;
+    uint32_t *alive = nullptr;        // [2n]          alive lists (ping-pong by level)
+    unsigned long long *gq = nullptr; // spill queues of work items (sentinel = ~0)
+    unsigned long long gq_cap = 0;    // capacity of each of the 3 x gq_nq queues
+    unsigned gq_nq = 0;
+    PeelTrace *trace = nullptr;       // per-level trace (when enabled)
+    uint32_t trace_cap = 0, trace_count = 0;
+    Tuning tune;
     bool gq_clean = false;            // gq holds only sentinels
     PeelCtl *peel_ctl = nullptr;
     uint32_t *list[2] = {nullptr, nullptr};  // h-index active lists

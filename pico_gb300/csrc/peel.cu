@@ -6,27 +6,30 @@
 //
 // State per vertex: deg[v] (residual degree; equals the core number when the
 // kernel returns) and one bit in `claimed` (v has been peeled).  Per level L:
-//   * scan: every CTA walks its private segment of still-alive vertices,
-//     claims those with deg <= L (atomicOr on the claim bit decides a unique
-//     owner), compacts the survivors in place and records min(deg) of them;
-//   * process: a claimed vertex's row is walked by one warp (rows above CHUNK
-//     entries are split into chunk items that any CTA may take).  Each
+//   * scan: CTAs take 512-vertex tiles of the global list of still-alive
+//     vertices from a shared cursor, claim those with deg <= L (atomicOr on
+//     the claim bit decides a unique owner), append the survivors to the next
+//     level's list (one atomicAdd per tile) and record min(deg) of them;
+//   * process: a claimed vertex's row is walked by one warp, several short
+//     rows per warp through a shuffle-based load balance; rows above CHUNK
+//     entries are split into chunk items that any CTA may take.  Each
 //     unclaimed neighbour u gets atomicSub(deg[u]); the thread that moves u
-//     from L+1 to L claims it and pushes it onto the CTA's shared-memory
-//     queue, so sub-level cascades run inside the level without any grid
-//     synchronisation (the reference repeats the level from the host or
-//     relies on a block-local queue with a 1e6-entry device assert).  A
-//     decrement that finds deg <= L is undone (the reference's clamp,
+//     from L+1 to L claims it and queues it, so sub-level cascades run inside
+//     the level without grid synchronisation (the reference repeats the level
+//     from the host, or uses a block-local queue guarded by a device assert).
+//     A decrement that finds deg <= L is undone (the reference's clamp,
 //     peelone.cu:80-86 / peelone-dyn.cc:95-98); values above L feed the
-//     next-level minimum.
+//     next-level minimum.  Each CTA keeps at most SPILL_T queued items in
+//     shared memory; the rest go to a global queue that idle CTAs steal from.
 //   * level skipping: the next level is the smallest residual degree seen,
 //     not L+1, so empty levels cost nothing.
 // Work accounting instead of a grid barrier: every level has a counter of
-// outstanding credits (one per CTA until its scan and queue are drained, plus
-// every item spilled to the global queue).  A level ends when the counter is
-// zero; idle CTAs steal spilled items meanwhile.  All waits are bounded by a
-// wall-clock limit and report KC_ERR_TIMEOUT instead of hanging.
+// outstanding credits (one per CTA until it finds no scan tile left and its
+// queue drained, plus every item put on the global queue).  A level ends when
+// the counter is zero.  All waits are bounded by a wall-clock limit and report
+// KC_ERR_TIMEOUT instead of hanging.
 #include <algorithm>
+#include <cstddef>
 
 #include "kc_device.cuh"
 #include "kc_internal.h"
@@ -36,8 +39,9 @@ namespace kc {
 constexpr int PEEL_THREADS = 512;
 constexpr int PEEL_WARPS = PEEL_THREADS / 32;
 constexpr unsigned QCAP = 4096;       // shared-memory queue capacity (items)
-constexpr unsigned LOW_WATER = 1024;  // scan a new tile only below this queue size
-constexpr unsigned CHUNK = 2048;      // row entries per work item
+constexpr unsigned LOW_WATER = 512;   // take a new scan tile only below this queue size
+constexpr unsigned MIN_CHUNK = 256;   // smallest row chunk (sizes the shared queues)
+constexpr int PEEL_U = 4;             // row entries in flight per lane
 constexpr unsigned long long SENT = ~0ull;
 constexpr unsigned int NO_LEVEL = 0xffffffffu;
 
@@ -49,12 +53,18 @@ struct PeelArgs {
     uint32_t n;
     uint32_t *deg;
     uint32_t *claimed;
-    uint32_t *alive;
-    unsigned long long *gq;
+    uint32_t *alive;  // two lists of n entries
+    unsigned long long *gq;      // 3 level slots x nq queues of gq_cap items
     unsigned long long gq_cap;
     PeelCtl *ctl;
+    PeelTrace *trace;            // per-level trace or nullptr
+    unsigned trace_cap;
     unsigned long long timeout_ns;
     uint32_t max_level_indices;
+    unsigned chunk;              // row entries per work item
+    unsigned spill_t;            // cascade items a CTA keeps locally
+    unsigned steal_max;          // items per steal
+    unsigned nq;                 // shared queues in use
 };
 
 __global__ void peel_init(const int64_t *__restrict__ rowptr, uint32_t n, uint32_t *deg, uint32_t *claimed,
@@ -67,11 +77,16 @@ __global__ void peel_init(const int64_t *__restrict__ rowptr, uint32_t n, uint32
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         for (int i = 0; i < 3; i++) {
             ctl->pending[i] = grid;
+            ctl->scan_cursor[i] = 0;
+            ctl->out_len[i] = 0;
             ctl->next_min[i] = NO_LEVEL;
             ctl->nonempty[i] = 0;
         }
-        ctl->gq_head = 0;
-        ctl->gq_tail = 0;
+        for (int sl = 0; sl < 3; sl++)
+            for (int i = 0; i < PEEL_MAX_QUEUES; i++) {
+                ctl->q[sl][i].head = 0;
+                ctl->q[sl][i].tail = 0;
+            }
         ctl->err = 0;
         ctl->err_info = 0;
         ctl->level_indices = 0;
@@ -96,11 +111,12 @@ __global__ void __launch_bounds__(PEEL_THREADS, 2) peel_kernel(PeelArgs A) {
     __shared__ unsigned int q_head, q_tail;
     __shared__ int mode;
     __shared__ unsigned int b_base, b_per_warp, b_take;
-    __shared__ unsigned int scan_pos, scan_len, write_pos, scan_done;
+    __shared__ unsigned long long tile_base, scan_len, out_base;
+    __shared__ unsigned int scan_done;
     __shared__ unsigned long long credit;
     __shared__ unsigned int min_sh, claimed_any;
     __shared__ unsigned long long steal_base;
-    __shared__ unsigned int steal_n;
+    __shared__ unsigned int steal_n, probe, claims_sh, spill_rr;
     __shared__ unsigned int level_sh, li_sh;
     __shared__ unsigned long long wait_t0;
     __shared__ unsigned int warp_cnt[PEEL_WARPS];
@@ -109,16 +125,14 @@ __global__ void __launch_bounds__(PEEL_THREADS, 2) peel_kernel(PeelArgs A) {
     const unsigned G = gridDim.x;
     PeelCtl *ctl = A.ctl;
     const uint32_t n = A.n;
-    const uint32_t seg = (uint32_t)(((uint64_t)n + G - 1) / G);
-    const uint64_t lo64 = (uint64_t)blockIdx.x * seg, hi64 = lo64 + seg;
-    const uint32_t seg_lo = (uint32_t)(lo64 < n ? lo64 : n);
-    const uint32_t seg_hi = (uint32_t)(hi64 < n ? hi64 : n);
 
     if (tid == 0) {
         q_head = q_tail = 0;
         level_sh = 0;
         li_sh = 0;
-        scan_len = seg_hi - seg_lo;
+        scan_len = n;
+        probe = blockIdx.x;
+        spill_rr = blockIdx.x;
     }
     __syncthreads();
 
@@ -126,16 +140,28 @@ __global__ void __launch_bounds__(PEEL_THREADS, 2) peel_kernel(PeelArgs A) {
         const unsigned li = li_sh;
         const unsigned L = level_sh;
         const unsigned s = li % 3;
+        const uint32_t *src = A.alive + (size_t)(li & 1) * n;
+        uint32_t *dst = A.alive + (size_t)((li + 1) & 1) * n;
         if (tid == 0) {
             if (blockIdx.x == 0 && li >= 1) {
                 unsigned s1 = (li + 1) % 3;
                 ctl->pending[s1] = G;
+                ctl->scan_cursor[s1] = 0;
+                ctl->out_len[s1] = 0;
                 ctl->next_min[s1] = NO_LEVEL;
                 ctl->nonempty[s1] = 0;
+                for (unsigned i = 0; i < A.nq; i++) {
+                    ctl->q[s1][i].head = 0;
+                    ctl->q[s1][i].tail = 0;
+                }
                 __threadfence();
             }
-            scan_pos = 0;
-            write_pos = 0;
+            if (A.trace && blockIdx.x == 0 && li < A.trace_cap) {
+                A.trace[li].t_start_ns = global_ns();
+                A.trace[li].level = L;
+                A.trace[li].scan_len = (unsigned)scan_len;
+            }
+            claims_sh = 0;
             scan_done = (scan_len == 0);
             credit = 1;  // this CTA's token for the level
             min_sh = NO_LEVEL;
@@ -146,13 +172,19 @@ __global__ void __launch_bounds__(PEEL_THREADS, 2) peel_kernel(PeelArgs A) {
 
         for (;;) {  // work loop of one level
             if (tid == 0) {
-                int md;
+                int md = 0;
                 unsigned qsize = q_tail - q_head;
-                if (ld_relaxed(&ctl->err) != 0) {
-                    md = M_EXIT;
-                } else if (!scan_done && qsize < LOW_WATER) {
-                    md = M_SCAN;
-                } else if (qsize > 0) {
+                if (ld_relaxed(&ctl->err) != 0) md = M_EXIT;
+                if (!md && !scan_done && qsize < LOW_WATER) {
+                    unsigned long long t = atomicAdd(&ctl->scan_cursor[s], (unsigned long long)PEEL_THREADS);
+                    if (t < scan_len) {
+                        tile_base = t;
+                        md = M_SCAN;
+                    } else {
+                        scan_done = 1;
+                    }
+                }
+                if (!md && qsize > 0) {
                     unsigned per = (qsize + PEEL_WARPS - 1) / PEEL_WARPS;
                     if (per > 32) per = 32;
                     unsigned take = min(qsize, per * PEEL_WARPS);
@@ -161,10 +193,15 @@ __global__ void __launch_bounds__(PEEL_THREADS, 2) peel_kernel(PeelArgs A) {
                     b_take = take;
                     q_head += take;
                     md = M_PROC;
-                } else {
+                }
+                if (!md) {
                     // idle: hand back the credits held, after publishing this
                     // CTA's level minimum and claim flag
                     if (credit > 0) {
+                        if (A.trace && li < A.trace_cap && claims_sh) {
+                            atomicAdd(&A.trace[li].claimed, claims_sh);
+                            claims_sh = 0;
+                        }
                         if (min_sh != NO_LEVEL) atomicMin(&ctl->next_min[s], min_sh);
                         if (claimed_any) {
                             ctl->nonempty[s] = 1u;
@@ -174,20 +211,32 @@ __global__ void __launch_bounds__(PEEL_THREADS, 2) peel_kernel(PeelArgs A) {
                         atomicAdd(&ctl->pending[s], (unsigned long long)(0ull - credit));
                         credit = 0;
                     }
-                    unsigned long long h = ld_relaxed64(&ctl->gq_head);
-                    unsigned long long t = ld_relaxed64(&ctl->gq_tail);
-                    if (t > A.gq_cap) t = A.gq_cap;  // an overflow was flagged; never read past the end
+                    // probe the shared queues, starting at a rotating index
                     md = M_SPIN;
-                    if (h < t) {
+                    bool seen = false;
+                    for (unsigned k = 0; k < A.nq && md == M_SPIN; k++) {
+                        const unsigned qi = (probe + k) % A.nq;
+                        unsigned long long h = ld_relaxed64(&ctl->q[s][qi].head);
+                        unsigned long long t = ld_relaxed64(&ctl->q[s][qi].tail);
+                        if (t > A.gq_cap) t = A.gq_cap;  // an overflow was flagged; never read past the end
+                        if (h >= t) continue;
+                        seen = true;
                         unsigned long long take = t - h;
-                        if (take > QCAP / 2) take = QCAP / 2;
-                        if (atomicCAS(&ctl->gq_head, h, h + take) == h) {
-                            steal_base = h;
+                        if (take > A.steal_max) take = A.steal_max;
+                        if (atomicCAS(&ctl->q[s][qi].head, h, h + take) == h) {
+                            steal_base = ((unsigned long long)s * A.nq + qi) * A.gq_cap + h;
                             steal_n = (unsigned)take;
                             credit += take;
                             md = M_STEAL;
                             wait_t0 = 0;
+                            probe = qi;
+                            if (A.trace && li < A.trace_cap) atomicAdd(&A.trace[li].steals, 1u);
+                        } else if (A.trace && li < A.trace_cap) {
+                            atomicAdd(&A.trace[li].steal_fail, 1u);
                         }
+                    }
+                    if (md != M_SPIN || seen) {
+                        if (md == M_SPIN) probe++;
                     } else if (ld_acquire64(&ctl->pending[s]) == 0ull) {
                         md = M_DONE;
                     } else {
@@ -206,7 +255,7 @@ __global__ void __launch_bounds__(PEEL_THREADS, 2) peel_kernel(PeelArgs A) {
             if (md == M_DONE || md == M_EXIT) break;
 
             if (md == M_SPIN) {
-                if (tid == 0) __nanosleep(200);
+                if (tid == 0) __nanosleep(100);
                 __syncthreads();
                 continue;
             }
@@ -240,14 +289,14 @@ __global__ void __launch_bounds__(PEEL_THREADS, 2) peel_kernel(PeelArgs A) {
             }
 
             if (md == M_SCAN) {
-                // ---- scan one tile of this CTA's alive segment ------------
-                const unsigned pos = scan_pos + tid;
+                // ---- scan one tile of the alive list -----------------------
+                const unsigned long long pos = tile_base + tid;
                 const bool inr = pos < scan_len;
                 uint32_t v = 0;
                 bool keep = false, take = false;
                 unsigned dkeep = NO_LEVEL;
                 if (inr) {
-                    v = (li == 0) ? seg_lo + pos : A.alive[seg_lo + pos];
+                    v = (li == 0) ? (uint32_t)pos : src[pos];
                     unsigned w = __ldcg(&A.claimed[v >> 5]);
                     unsigned bit = 1u << (v & 31);
                     if (!(w & bit)) {
@@ -265,11 +314,13 @@ __global__ void __launch_bounds__(PEEL_THREADS, 2) peel_kernel(PeelArgs A) {
                 if (lane == 0 && dkeep != NO_LEVEL) atomicMin(&min_sh, dkeep);
                 // a claimed vertex with an empty row needs no processing
                 const bool push = take && (A.rowptr[v + 1] != A.rowptr[v]);
-                // survivors: in-place compaction (write index <= read index)
                 unsigned kb = __ballot_sync(KC_FULL_MASK, keep);
                 unsigned cb = __ballot_sync(KC_FULL_MASK, push);
                 const unsigned tb = __ballot_sync(KC_FULL_MASK, take);
-                if (lane == 0 && tb != 0u) claimed_any = 1;
+                if (lane == 0 && tb != 0u) {
+                    claimed_any = 1;
+                    if (A.trace) atomicAdd(&claims_sh, (unsigned)__popc(tb));
+                }
                 if (lane == 0) warp_cnt[warp] = __popc(kb) | (__popc(cb) << 16);
                 __syncthreads();
                 unsigned kofs = 0, cofs = 0, ktot = 0, ctot = 0;
@@ -282,16 +333,13 @@ __global__ void __launch_bounds__(PEEL_THREADS, 2) peel_kernel(PeelArgs A) {
                     ktot += x & 0xffffu;
                     ctot += x >> 16;
                 }
+                if (tid == 0 && ktot) out_base = atomicAdd(&ctl->out_len[s], (unsigned long long)ktot);
+                __syncthreads();
                 const unsigned lt = (1u << lane) - 1u;
-                if (keep) A.alive[seg_lo + write_pos + kofs + __popc(kb & lt)] = v;
+                if (keep) dst[out_base + kofs + __popc(kb & lt)] = v;
                 if (push) q[(q_tail + cofs + __popc(cb & lt)) % QCAP] = ((unsigned long long)v << 32);
                 __syncthreads();
-                if (tid == 0) {
-                    write_pos += ktot;
-                    q_tail += ctot;
-                    scan_pos += PEEL_THREADS;
-                    if (scan_pos >= scan_len) scan_done = 1;
-                }
+                if (tid == 0) q_tail += ctot;
                 __syncthreads();
                 continue;
             }
@@ -305,113 +353,153 @@ __global__ void __launch_bounds__(PEEL_THREADS, 2) peel_kernel(PeelArgs A) {
                 if (lane < nit) item = q[(my_lo + lane) % QCAP];
                 int64_t rs = 0;
                 uint32_t len = 0;
+                bool hub = false;
                 if (item != SENT) {
                     uint32_t v = (uint32_t)(item >> 32);
                     uint32_t c = (uint32_t)item;
                     int64_t r0 = A.rowptr[v], r1 = A.rowptr[v + 1];
-                    rs = r0 + (int64_t)c * CHUNK;
-                    int64_t re = min(r1, rs + (int64_t)CHUNK);
+                    rs = r0 + (int64_t)c * A.chunk;
+                    int64_t re = min(r1, rs + (int64_t)A.chunk);
                     len = re > rs ? (uint32_t)(re - rs) : 0u;
-                    if (c == 0 && r1 - r0 > (int64_t)CHUNK) item |= 1ull << 31;  // mark: split needed
+                    hub = (c == 0 && r1 - r0 > (int64_t)A.chunk);
                 }
                 // split hub rows: chunk items 1..k-1 go to the global queue
-                unsigned hubs = __ballot_sync(KC_FULL_MASK, item != SENT && (item & (1ull << 31)));
+                unsigned hubs = __ballot_sync(KC_FULL_MASK, hub);
                 while (hubs) {
-                    const int src = __ffs(hubs) - 1;
+                    const int srcl = __ffs(hubs) - 1;
                     hubs &= hubs - 1;
-                    unsigned long long hi = __shfl_sync(KC_FULL_MASK, item, src);
+                    unsigned long long hi = __shfl_sync(KC_FULL_MASK, item, srcl);
                     uint32_t v = (uint32_t)(hi >> 32);
                     int64_t d = A.rowptr[v + 1] - A.rowptr[v];
-                    unsigned k = (unsigned)((d + CHUNK - 1) / CHUNK);
+                    unsigned k = (unsigned)((d + A.chunk - 1) / A.chunk);
                     unsigned extra = k - 1;
-                    unsigned long long pos = 0;
-                    if (lane == 0) {
-                        atomicAdd(&ctl->pending[s], (unsigned long long)extra);
-                        __threadfence();
-                        pos = atomicAdd(&ctl->gq_tail, (unsigned long long)extra);
-                        if (pos + extra > A.gq_cap) set_err(ctl, KC_ERR_CAPACITY, 3);
+                    // spread the chunks over the shared queues, 32 per queue
+                    for (unsigned c0 = 0; c0 < extra; c0 += 32) {
+                        const unsigned cnt = min(32u, extra - c0);
+                        unsigned qi = 0;
+                        if (lane == 0) qi = atomicAdd(&spill_rr, 1u) % A.nq;
+                        qi = __shfl_sync(KC_FULL_MASK, qi, 0);
+                        unsigned long long pos = 0;
+                        if (lane == 0) {
+                            atomicAdd(&ctl->pending[s], (unsigned long long)cnt);
+                            __threadfence();
+                            pos = atomicAdd(&ctl->q[s][qi].tail, (unsigned long long)cnt);
+                            if (pos + cnt > A.gq_cap) set_err(ctl, KC_ERR_CAPACITY, 3);
+                            if (A.trace && li < A.trace_cap) atomicAdd(&A.trace[li].spilled, cnt);
+                        }
+                        pos = __shfl_sync(KC_FULL_MASK, pos, 0);
+                        if (lane < cnt && pos + cnt <= A.gq_cap)
+                            st_relaxed64(&A.gq[((unsigned long long)s * A.nq + qi) * A.gq_cap + pos + lane],
+                                         ((unsigned long long)v << 32) | (c0 + lane + 1));
                     }
-                    pos = __shfl_sync(KC_FULL_MASK, pos, 0);
-                    if (pos + extra <= A.gq_cap)
-                        for (unsigned j = lane; j < extra; j += 32)
-                            st_relaxed64(&A.gq[pos + j], ((unsigned long long)v << 32) | (j + 1));
                 }
-                // expand the concatenated rows of this warp's items
+                // expand the concatenated rows of this warp's items; each lane
+                // keeps PEEL_U entries in flight (loads, then bitmap probes,
+                // then decrements) so the round trips overlap
                 unsigned total;
                 unsigned off = warp_excl_scan(len, lane, total);
+                const bool single = __ballot_sync(KC_FULL_MASK, len != 0) == 1u;  // one item, in lane 0
                 unsigned local_min = NO_LEVEL;
-                for (unsigned base = 0; base < total; base += 32) {
-                    const unsigned e = base + lane;
-                    bool push = false;
-                    uint32_t u = 0;
-                    // owner = last lane j with off_j <= e
-                    unsigned j = 0;
+                unsigned wclaims = 0;
+                for (unsigned base = 0; base < total; base += 32 * PEEL_U) {
+                    uint32_t u[PEEL_U];
+                    unsigned a[PEEL_U];
+                    bool live[PEEL_U];
 #pragma unroll
-                    for (unsigned step = 16; step > 0; step >>= 1) {
-                        unsigned cand = j + step;
-                        unsigned oc = __shfl_sync(KC_FULL_MASK, off, cand & 31);
-                        if (cand < 32 && oc <= e) j = cand;
+                    for (int k = 0; k < PEEL_U; k++) {
+                        const unsigned e = base + k * 32 + lane;
+                        int64_t rj;
+                        unsigned oj;
+                        if (single) {
+                            rj = __shfl_sync(KC_FULL_MASK, rs, 0);
+                            oj = 0;
+                        } else {
+                            // owner = last lane j with off_j <= e
+                            unsigned j = 0;
+#pragma unroll
+                            for (unsigned step = 16; step > 0; step >>= 1) {
+                                unsigned cand = j + step;
+                                unsigned oc = __shfl_sync(KC_FULL_MASK, off, cand & 31);
+                                if (cand < 32 && oc <= e) j = cand;
+                            }
+                            rj = __shfl_sync(KC_FULL_MASK, rs, j);
+                            oj = __shfl_sync(KC_FULL_MASK, off, j);
+                        }
+                        live[k] = e < total;
+                        u[k] = live[k] ? __ldcs(&A.col[rj + (e - oj)]) : 0u;
                     }
-                    int64_t rj = __shfl_sync(KC_FULL_MASK, rs, j);
-                    unsigned oj = __shfl_sync(KC_FULL_MASK, off, j);
-                    if (e < total) {
-                        u = __ldcs(&A.col[rj + (e - oj)]);
-                        const unsigned bit = 1u << (u & 31);
-                        unsigned w = __ldcg(&A.claimed[u >> 5]);
-                        if (!(w & bit)) {
-                            unsigned a = atomicSub(&A.deg[u], 1u);
-                            if (a == L + 1) {
-                                unsigned old = atomicOr(&A.claimed[u >> 5], bit);
+#pragma unroll
+                    for (int k = 0; k < PEEL_U; k++) {
+                        if (live[k]) {
+                            unsigned w = __ldcg(&A.claimed[u[k] >> 5]);
+                            live[k] = !(w & (1u << (u[k] & 31)));
+                        }
+                    }
+#pragma unroll
+                    for (int k = 0; k < PEEL_U; k++) a[k] = live[k] ? atomicSub(&A.deg[u[k]], 1u) : 0u;
+#pragma unroll
+                    for (int k = 0; k < PEEL_U; k++) {
+                        bool push = false;
+                        if (live[k]) {
+                            if (a[k] == L + 1) {
+                                const unsigned bit = 1u << (u[k] & 31);
+                                unsigned old = atomicOr(&A.claimed[u[k] >> 5], bit);
                                 push = !(old & bit);
-                            } else if ((int)a <= (int)L) {
-                                atomicAdd(&A.deg[u], 1u);
+                            } else if ((int)a[k] <= (int)L) {
+                                atomicAdd(&A.deg[u[k]], 1u);
                             } else {
-                                local_min = min(local_min, a - 1);
+                                local_min = min(local_min, a[k] - 1);
                             }
                         }
-                    }
-                    unsigned pb = __ballot_sync(KC_FULL_MASK, push);
-                    if (pb) {
-                        // claimed neighbours: append to the CTA queue, or spill
-                        // to the global queue when the ring would overwrite
-                        // items of this step's batch (which starts at b_base)
-                        const unsigned cnt = __popc(pb);
-                        unsigned slot_lo = 0, slot_hi = 0;
-                        int spill = 0;
-                        if (lane == 0) {
-                            unsigned t = q_tail;
-                            for (;;) {
-                                if (t + cnt - b_base > QCAP) { spill = 1; break; }
-                                unsigned old = atomicCAS(&q_tail, t, t + cnt);
-                                if (old == t) break;
-                                t = old;
+                        unsigned pb = __ballot_sync(KC_FULL_MASK, push);
+                        wclaims += __popc(pb);
+                        if (pb) {
+                            // claimed neighbours: append to the CTA queue while it
+                            // holds fewer than spill_t items (and the ring would not
+                            // overwrite this step's batch, which starts at b_base);
+                            // otherwise publish them on a shared queue
+                            const unsigned cnt = __popc(pb);
+                            unsigned slot_lo = 0, slot_hi = 0;
+                            int spill = 0;
+                            if (lane == 0) {
+                                unsigned t = q_tail;
+                                for (;;) {
+                                    if (t + cnt - b_base > QCAP || t + cnt - q_head > A.spill_t) { spill = 1; break; }
+                                    unsigned old = atomicCAS(&q_tail, t, t + cnt);
+                                    if (old == t) break;
+                                    t = old;
+                                }
+                                unsigned long long p = t;
+                                if (spill) {
+                                    const unsigned qi = atomicAdd(&spill_rr, 1u) % A.nq;
+                                    atomicAdd(&ctl->pending[s], (unsigned long long)cnt);
+                                    __threadfence();
+                                    p = atomicAdd(&ctl->q[s][qi].tail, (unsigned long long)cnt);
+                                    if (p + cnt > A.gq_cap) { set_err(ctl, KC_ERR_CAPACITY, 4); spill = 2; }
+                                    p += ((unsigned long long)s * A.nq + qi) * A.gq_cap;
+                                    if (A.trace && li < A.trace_cap) atomicAdd(&A.trace[li].spilled, cnt);
+                                }
+                                slot_lo = (unsigned)p;
+                                slot_hi = (unsigned)(p >> 32);
                             }
-                            unsigned long long p = t;
-                            if (spill) {
-                                atomicAdd(&ctl->pending[s], (unsigned long long)cnt);
-                                __threadfence();
-                                p = atomicAdd(&ctl->gq_tail, (unsigned long long)cnt);
-                                if (p + cnt > A.gq_cap) { set_err(ctl, KC_ERR_CAPACITY, 4); spill = 2; }
+                            spill = __shfl_sync(KC_FULL_MASK, spill, 0);
+                            slot_lo = __shfl_sync(KC_FULL_MASK, slot_lo, 0);
+                            slot_hi = __shfl_sync(KC_FULL_MASK, slot_hi, 0);
+                            const unsigned r = __popc(pb & ((1u << lane) - 1u));
+                            if (push) {
+                                const unsigned long long itm = (unsigned long long)u[k] << 32;
+                                if (spill == 0)
+                                    q[(slot_lo + r) % QCAP] = itm;
+                                else if (spill == 1)
+                                    st_relaxed64(&A.gq[(((unsigned long long)slot_hi << 32) | slot_lo) + r], itm);
                             }
-                            slot_lo = (unsigned)p;
-                            slot_hi = (unsigned)(p >> 32);
-                        }
-                        spill = __shfl_sync(KC_FULL_MASK, spill, 0);
-                        slot_lo = __shfl_sync(KC_FULL_MASK, slot_lo, 0);
-                        slot_hi = __shfl_sync(KC_FULL_MASK, slot_hi, 0);
-                        const unsigned r = __popc(pb & ((1u << lane) - 1u));
-                        if (push) {
-                            const unsigned long long itm = (unsigned long long)u << 32;
-                            if (spill == 0)
-                                q[(slot_lo + r) % QCAP] = itm;
-                            else if (spill == 1)
-                                st_relaxed64(&A.gq[(((unsigned long long)slot_hi << 32) | slot_lo) + r], itm);
                         }
                     }
                 }
                 local_min = __reduce_min_sync(KC_FULL_MASK, local_min);
                 if (lane == 0 && local_min != NO_LEVEL) atomicMin(&min_sh, local_min);
                 if (lane == 0 && nit) claimed_any = 1;
+                if (A.trace && lane == 0 && wclaims) atomicAdd(&claims_sh, wclaims);
             }
             __syncthreads();
         }
@@ -423,6 +511,7 @@ __global__ void __launch_bounds__(PEEL_THREADS, 2) peel_kernel(PeelArgs A) {
             if (mode == M_DONE) {
                 __threadfence();
                 nxt = ld_acquire(&ctl->next_min[s]);
+                scan_len = ld_acquire64(&ctl->out_len[s]);
                 if (blockIdx.x == 0) {
                     ctl->level_indices = li + 1;
                     if (ld_relaxed(&ctl->nonempty[s])) ctl->levels += 1;
@@ -432,7 +521,6 @@ __global__ void __launch_bounds__(PEEL_THREADS, 2) peel_kernel(PeelArgs A) {
                     nxt = NO_LEVEL;
                 }
             }
-            scan_len = write_pos;
             level_sh = nxt;
             li_sh = li + 1;
         }
@@ -446,24 +534,44 @@ static int ensure_peel_buffers(Graph *g) {
     const uint64_t n = g->n;
     if (!g->core) KC_TRY(dalloc(&g->core, n + 1, "core"));
     if (!g->bitmap) KC_TRY(dalloc(&g->bitmap, (n + 31) / 32 + 1, "claim bitmap"));
-    if (!g->alive) KC_TRY(dalloc(&g->alive, n + 1, "alive lists"));
-    if (!g->gq) {
-        g->gq_cap = 2 * n + g->nnz / CHUNK + 4096;
-        KC_TRY(dalloc(&g->gq, g->gq_cap, "spill queue"));
+    if (!g->alive) KC_TRY(dalloc(&g->alive, 2 * n + 2, "alive lists"));
+    const unsigned nq = (unsigned)g->tune.peel_queues;
+    if (!g->gq || g->gq_nq != nq) {
+        // Pushes per level <= n (each vertex is claimed once) + nnz/MIN_CHUNK
+        // (row chunks).  Every CTA rotates over the queues one push (<= 32
+        // items) at a time, so a queue receives at most total/nq + 32 items
+        // per CTA.  Each level slot (3) has its own queues, restarted at 0
+        // when the slot is recycled; consumed entries are reset to SENT.
+        dfree(g->gq);
+        g->gq = nullptr;
+        const unsigned long long total = n + g->nnz / MIN_CHUNK + 64;
+        const unsigned long long ctas = (unsigned long long)g->sm_count * 4;
+        g->gq_cap = total / nq + 32 * ctas + 8192;
+        KC_TRY(dalloc(&g->gq, 3 * g->gq_cap * nq, "spill queues"));
+        g->gq_nq = nq;
         g->gq_clean = false;
+    }
+    if (g->tune.trace && (!g->trace || g->trace_cap < g->max_deg + 3)) {
+        dfree(g->trace);
+        g->trace = nullptr;
+        g->trace_cap = g->max_deg + 3;
+        KC_TRY(dalloc(&g->trace, g->trace_cap, "peel trace"));
     }
     if (!g->peel_ctl) KC_TRY(dalloc(&g->peel_ctl, 1, "peel control"));
     return KC_OK;
 }
 
-static int peel_grid(int sm_count, int *grid) {
+static int peel_grid(int sm_count, int ctas_per_sm, int *grid) {
     int occ = 0;
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, peel_kernel, PEEL_THREADS, 0);
     if (e != cudaSuccess) return fail(KC_ERR_CUDA, "occupancy query: %s", cudaGetErrorString(e));
     if (occ < 1) return fail(KC_ERR_UNSUPPORTED, "peel kernel cannot be resident");
+    if (ctas_per_sm > 0 && ctas_per_sm < occ) occ = ctas_per_sm;
     *grid = occ * sm_count;
     return KC_OK;
 }
+
+static unsigned nq_of(const Graph *g) { return g->gq_nq; }
 
 int peel_run(Graph *g, cudaStream_t s, bool gpp_zero_to_one_flag, kc_stats *st) {
     KC_TRY(ensure_peel_buffers(g));
@@ -471,9 +579,9 @@ int peel_run(Graph *g, cudaStream_t s, bool gpp_zero_to_one_flag, kc_stats *st) 
     cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, g->device);
     if (!coop) return fail(KC_ERR_UNSUPPORTED, "device lacks cooperative launch");
     int grid = 0;
-    KC_TRY(peel_grid(g->sm_count, &grid));
+    KC_TRY(peel_grid(g->sm_count, g->tune.peel_ctas_per_sm, &grid));
     if (!g->gq_clean) {
-        KC_CUDA(cudaMemsetAsync(g->gq, 0xff, g->gq_cap * sizeof(unsigned long long), s));
+        KC_CUDA(cudaMemsetAsync(g->gq, 0xff, 3 * g->gq_cap * g->gq_nq * sizeof(unsigned long long), s));
         g->gq_clean = true;
     }
     if (!g->ev0) {
@@ -492,9 +600,16 @@ int peel_run(Graph *g, cudaStream_t s, bool gpp_zero_to_one_flag, kc_stats *st) 
     A.gq = g->gq;
     A.gq_cap = g->gq_cap;
     A.ctl = g->peel_ctl;
+    A.trace = g->tune.trace ? g->trace : nullptr;
+    A.trace_cap = g->tune.trace ? g->trace_cap : 0;
     A.timeout_ns = 20ull * 1000 * 1000 * 1000;
     A.max_level_indices = g->max_deg + 3;
+    A.chunk = (unsigned)g->tune.peel_chunk;
+    A.spill_t = (unsigned)g->tune.peel_spill;
+    A.steal_max = (unsigned)g->tune.peel_steal;
+    A.nq = nq_of(g);
     KC_CUDA(cudaEventRecord(g->ev0, s));
+    if (A.trace) KC_CUDA(cudaMemsetAsync(g->trace, 0, sizeof(PeelTrace) * g->trace_cap, s));
     const int ig = std::max(1, std::min<int>(g->sm_count * 8, (int)((g->n + 255) / 256)));
     peel_init<<<ig, 256, 0, s>>>(g->rowptr, g->n, g->core, g->bitmap, g->peel_ctl, (unsigned)grid);
     void *args[] = {&A};
@@ -505,7 +620,7 @@ int peel_run(Graph *g, cudaStream_t s, bool gpp_zero_to_one_flag, kc_stats *st) 
         gpp_zero_to_one<<<ig, 256, 0, s>>>(g->rowptr, g->n, g->core);
     KC_CUDA(cudaEventRecord(g->ev1, s));
     PeelCtl h;
-    KC_CUDA(cudaMemcpyAsync(&h, g->peel_ctl, sizeof(h), cudaMemcpyDeviceToHost, s));
+    KC_CUDA(cudaMemcpyAsync(&h, g->peel_ctl, offsetof(PeelCtl, q), cudaMemcpyDeviceToHost, s));
     KC_CUDA(cudaStreamSynchronize(s));
     float ms = 0.f, kms = 0.f;
     cudaEventElapsedTime(&ms, g->ev0, g->ev1);
@@ -518,6 +633,7 @@ int peel_run(Graph *g, cudaStream_t s, bool gpp_zero_to_one_flag, kc_stats *st) 
         return fail((int)h.err, "peel kernel raised error %u at site %u", h.err, h.err_info);
     }
     g->core_valid = true;
+    g->trace_count = A.trace ? std::min<uint32_t>(h.level_indices, g->trace_cap) : 0;
     if (st) {
         st->iterations = h.level_indices;
         st->levels = h.levels;

@@ -1,0 +1,62 @@
+"""The peel's work-accounting protocol under extreme tunables: everything
+spilled to the shared queues, one item per steal, 1..64 queues, tiny and large
+row chunks, one CTA per SM.  Every setting must give the exact core numbers."""
+import numpy as np
+import pytest
+
+import oracle
+import pico_gb300 as pg
+
+pytestmark = pytest.mark.gpu
+
+SETTINGS = [
+    {},
+    {"peel.queues": 1},
+    {"peel.queues": 64, "peel.steal": 1},
+    {"peel.spill": 0, "peel.steal": 3},
+    {"peel.spill": 0, "peel.queues": 7, "peel.chunk": 256},
+    {"peel.spill": 3072, "peel.steal": 2048, "peel.chunk": 65536},
+    {"peel.ctas_per_sm": 1, "peel.queues": 32},
+    {"peel.chunk": 256, "peel.steal": 5, "peel.queues": 3},
+]
+
+
+def graphs():
+    yield "rmat16", pg.rmat_graph(16, 16, seed=11)
+    rng = np.random.default_rng(4)
+    n = 50000
+    s = np.concatenate([np.arange(n - 1), rng.integers(0, n, 20000)]).astype(np.uint32)
+    d = np.concatenate([np.arange(1, n), rng.integers(0, n, 20000)]).astype(np.uint32)
+    yield "path+random", pg.Graph.from_edges(s, d, n, dedup=True)
+    k = 400
+    a, b = np.triu_indices(k, 1)
+    hub = np.arange(k, 30000, dtype=np.uint32)
+    s = np.concatenate([a, np.zeros(hub.size)]).astype(np.uint32)
+    d = np.concatenate([b, hub]).astype(np.uint32)
+    yield "clique+star", pg.Graph.from_edges(s, d, 30000, dedup=True)
+
+
+@pytest.mark.parametrize("setting", SETTINGS, ids=lambda p: ",".join("%s=%d" % kv for kv in p.items()) or "default")
+def test_peel_exact_under_tunables(setting):
+    for name, g in graphs():
+        rp, col = g.csr()
+        core, _ = oracle.bz(rp, col)
+        for k, v in setting.items():
+            g.set_param(k, v)
+        for method in ("peelone_dyn", "gppeel"):
+            got, st = g.decompose(method)
+            want = np.where(np.diff(rp) == 0, 1, core) if method == "gppeel" else core
+            assert np.array_equal(got, want), (name, method, setting)
+        g.free()
+
+
+def test_trace_records_levels():
+    g = pg.rmat_graph(15, 8, seed=5)
+    g.set_param("trace", 1)
+    core, st = g.decompose("peelone_dyn")
+    tr = g.trace()
+    assert len(tr) == st.iterations
+    assert sum(r["claimed"] for r in tr) == g.n
+    levels = [r["level"] for r in tr]
+    assert levels == sorted(levels) and levels[0] == 0
+    assert len({r["level"] for r in tr if r["claimed"]}) == st.levels == np.unique(core).size

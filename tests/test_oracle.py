@@ -121,3 +121,10 @@ def test_hindex_iteration_counts_match_reference_trajectory(golden):
     col = np.array(case["csr"]["neighbors"], dtype=np.uint32)
     assert oracle.hindex_jacobi(rp, col)[1] == 3
     assert oracle.peel_dyn(rp, col)[1] == 3  # levels 0, 1, 2
+
+
+def test_rmat_restatements_agree():
+    from oracle import gen
+    s1, d1 = gen.rmat_numpy(16, 5000, 9)
+    s2, d2 = gen.rmat(16, (1 << 20) + 7, 9)
+    assert np.array_equal(s1, s2[:5000]) and np.array_equal(d1, d2[:5000])
