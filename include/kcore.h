@@ -174,7 +174,7 @@ int kc_graph_last_timing(const kc_graph *g, double *total_ms, double *kernel_ms)
 /* Tunables of the decomposition kernels, set per graph (the autotuner and
  * the benchmarks use these).  Names: "peel.chunk" (row entries per peel work
  * item), "peel.spill" (cascade items a CTA keeps before publishing to the
- * shared queues), "peel.steal" (items taken per steal), "peel.queues" (number
+ * shared queues), "peel.steal" (most items reserved per steal, 1..64), "peel.queues" (number
  * of shared queues, 1..64), "peel.ctas_per_sm" (0 = occupancy maximum),
  * "trace" (1 = record a per-level trace of the next decompositions). */
 int kc_graph_set_param(kc_graph *g, const char *name, int64_t value);

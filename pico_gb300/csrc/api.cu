@@ -379,7 +379,7 @@ int kc_graph_set_param(kc_graph *g, const char *name, int64_t value) {
         if (value < 0 || value > 3072) return fail(KC_ERR_INVALID, "peel.spill: [0, 3072]");
         t.peel_spill = (int)value;
     } else if (k == "peel.steal") {
-        if (value < 1 || value > 2048) return fail(KC_ERR_INVALID, "peel.steal: [1, 2048]");
+        if (value < 1 || value > 64) return fail(KC_ERR_INVALID, "peel.steal: [1, 64]");
         t.peel_steal = (int)value;
     } else if (k == "peel.queues") {
         if (value < 1 || value > PEEL_MAX_QUEUES) return fail(KC_ERR_INVALID, "peel.queues: [1, %d]", PEEL_MAX_QUEUES);

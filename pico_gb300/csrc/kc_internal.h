@@ -73,10 +73,10 @@ struct PeelTrace {
 };
 
 struct Tuning {
-    int peel_chunk = 512;
+    int peel_chunk = 256;
     int peel_spill = 32;
     int peel_steal = 64;
-    int peel_queues = 16;
+    int peel_queues = 1;
     int peel_ctas_per_sm = 0;
     int trace = 0;
 };

@@ -39,7 +39,9 @@ namespace kc {
 constexpr int PEEL_THREADS = 512;
 constexpr int PEEL_WARPS = PEEL_THREADS / 32;
 constexpr unsigned QCAP = 4096;       // shared-memory queue capacity (items)
-constexpr unsigned LOW_WATER = 512;   // take a new scan tile only below this queue size
+constexpr unsigned LOW_WATER = 1024;  // take a new scan tile only below this queue size
+constexpr int SCAN_U = 4;             // alive-list entries per thread per scan tile
+constexpr unsigned TILE = PEEL_THREADS * SCAN_U;
 constexpr unsigned MIN_CHUNK = 256;   // smallest row chunk (sizes the shared queues)
 constexpr int PEEL_U = 4;             // row entries in flight per lane
 constexpr unsigned long long SENT = ~0ull;
@@ -67,32 +69,72 @@ struct PeelArgs {
     unsigned nq;                 // shared queues in use
 };
 
+// Initialisation and level 0 in one streaming pass: residual degrees from the
+// row offsets; degree-0 vertices are peeled at level 0 (their claim bits are
+// written whole, one warp ballot per 32-vertex word); every other vertex is
+// appended to the alive list that level index 1 scans, and the smallest
+// degree among them becomes level index 1's level.
 __global__ void peel_init(const int64_t *__restrict__ rowptr, uint32_t n, uint32_t *deg, uint32_t *claimed,
-                          PeelCtl *ctl, unsigned int grid) {
-    uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n; v += stride)
-        deg[v] = (uint32_t)(rowptr[v + 1] - rowptr[v]);
-    uint64_t words = ((uint64_t)n + 31) / 32;
-    for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < words; w += stride) claimed[w] = 0u;
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        for (int i = 0; i < 3; i++) {
-            ctl->pending[i] = grid;
-            ctl->scan_cursor[i] = 0;
-            ctl->out_len[i] = 0;
-            ctl->next_min[i] = NO_LEVEL;
-            ctl->nonempty[i] = 0;
+                          uint32_t *alive1, PeelCtl *ctl, unsigned int grid) {
+    __shared__ unsigned int wcnt[32];
+    __shared__ unsigned long long base_sh;
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    unsigned dmin = 0xffffffffu;
+    bool any_zero = false;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t b0 = (uint64_t)blockIdx.x * blockDim.x; b0 < n; b0 += stride) {
+        const uint64_t v = b0 + threadIdx.x;  // b0 is a multiple of 32: a warp covers one bitmap word
+        uint32_t d = 0;
+        const bool inr = v < n;
+        if (inr) {
+            d = (uint32_t)(rowptr[v + 1] - rowptr[v]);
+            deg[v] = d;
         }
-        for (int sl = 0; sl < 3; sl++)
-            for (int i = 0; i < PEEL_MAX_QUEUES; i++) {
-                ctl->q[sl][i].head = 0;
-                ctl->q[sl][i].tail = 0;
+        const unsigned zero = __ballot_sync(KC_FULL_MASK, inr && d == 0);
+        if (lane == 0 && v < n) claimed[v >> 5] = zero;
+        any_zero |= zero != 0u;
+        const bool keep = inr && d != 0;
+        if (keep) dmin = min(dmin, d);
+        const unsigned kb = __ballot_sync(KC_FULL_MASK, keep);
+        if (lane == 0) wcnt[warp] = __popc(kb);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned tot = 0;
+            for (unsigned w = 0; w < nw; w++) {
+                unsigned c = wcnt[w];
+                wcnt[w] = tot;
+                tot += c;
             }
-        ctl->err = 0;
-        ctl->err_info = 0;
-        ctl->level_indices = 0;
-        ctl->levels = 0;
-        ctl->kmax = 0;
+            base_sh = tot ? atomicAdd(&ctl->out_len[0], (unsigned long long)tot) : 0ull;
+        }
+        __syncthreads();
+        if (keep) alive1[base_sh + wcnt[warp] + __popc(kb & ((1u << lane) - 1u))] = (uint32_t)v;
+        __syncthreads();
     }
+    dmin = __reduce_min_sync(KC_FULL_MASK, dmin);
+    if (lane == 0 && dmin != 0xffffffffu) atomicMin(&ctl->next_min[0], dmin);
+    if (__any_sync(KC_FULL_MASK, any_zero) && lane == 0) atomicExch(&ctl->nonempty[0], 1u);
+}
+
+// Resets the control block before peel_init runs.
+__global__ void peel_ctl_reset(PeelCtl *ctl, unsigned int grid) {
+    for (int i = 0; i < 3; i++) {
+        ctl->pending[i] = grid;
+        ctl->scan_cursor[i] = 0;
+        ctl->out_len[i] = 0;
+        ctl->next_min[i] = NO_LEVEL;
+        ctl->nonempty[i] = 0;
+    }
+    for (int sl = 0; sl < 3; sl++)
+        for (int i = 0; i < PEEL_MAX_QUEUES; i++) {
+            ctl->q[sl][i].head = 0;
+            ctl->q[sl][i].tail = 0;
+        }
+    ctl->err = 0;
+    ctl->err_info = 0;
+    ctl->level_indices = 0;
+    ctl->levels = 0;
+    ctl->kmax = 0;
 }
 
 // Degree-0 vertices get core 1 in GPP mode (gppeel.cu:247-252: its first
@@ -115,11 +157,12 @@ __global__ void __launch_bounds__(PEEL_THREADS, 2) peel_kernel(PeelArgs A) {
     __shared__ unsigned int scan_done;
     __shared__ unsigned long long credit;
     __shared__ unsigned int min_sh, claimed_any;
-    __shared__ unsigned long long steal_base;
-    __shared__ unsigned int steal_n, probe, claims_sh, spill_rr;
+    __shared__ unsigned long long res_base, res_mask;  // reserved queue slots still expected
+    __shared__ unsigned int steal_cnt, probe, claims_sh, spill_rr;
     __shared__ unsigned int level_sh, li_sh;
     __shared__ unsigned long long wait_t0;
-    __shared__ unsigned int warp_cnt[PEEL_WARPS];
+    __shared__ unsigned int warp_cnt[SCAN_U][PEEL_WARPS];
+    __shared__ unsigned long long next_tile;
 
     const unsigned tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const unsigned G = gridDim.x;
@@ -127,14 +170,33 @@ __global__ void __launch_bounds__(PEEL_THREADS, 2) peel_kernel(PeelArgs A) {
     const uint32_t n = A.n;
 
     if (tid == 0) {
+        // level index 0 (the degree-0 vertices) was done by peel_init
         q_head = q_tail = 0;
-        level_sh = 0;
-        li_sh = 0;
-        scan_len = n;
+        level_sh = ld_acquire(&ctl->next_min[0]);
+        li_sh = 1;
+        scan_len = ld_relaxed64(&ctl->out_len[0]);
         probe = blockIdx.x;
         spill_rr = blockIdx.x;
+        res_mask = 0;
+        steal_cnt = 0;
     }
     __syncthreads();
+    if (level_sh == NO_LEVEL) {  // every vertex had degree 0
+        if (blockIdx.x == 0 && tid == 0) {
+            ctl->level_indices = 1;
+            ctl->levels = ld_relaxed(&ctl->nonempty[0]) ? 1u : 0u;
+        }
+        return;
+    }
+    if (blockIdx.x == 0 && tid == 0) {
+        if (ld_relaxed(&ctl->nonempty[0])) ctl->levels = 1;
+        if (A.trace && A.trace_cap) {
+            A.trace[0].t_start_ns = global_ns();
+            A.trace[0].level = 0;
+            A.trace[0].scan_len = n;
+            A.trace[0].claimed = n - (unsigned)scan_len;
+        }
+    }
 
     for (;;) {  // level loop
         const unsigned li = li_sh;
@@ -143,7 +205,7 @@ __global__ void __launch_bounds__(PEEL_THREADS, 2) peel_kernel(PeelArgs A) {
         const uint32_t *src = A.alive + (size_t)(li & 1) * n;
         uint32_t *dst = A.alive + (size_t)((li + 1) & 1) * n;
         if (tid == 0) {
-            if (blockIdx.x == 0 && li >= 1) {
+            if (blockIdx.x == 0) {
                 unsigned s1 = (li + 1) % 3;
                 ctl->pending[s1] = G;
                 ctl->scan_cursor[s1] = 0;
@@ -162,6 +224,7 @@ __global__ void __launch_bounds__(PEEL_THREADS, 2) peel_kernel(PeelArgs A) {
                 A.trace[li].scan_len = (unsigned)scan_len;
             }
             claims_sh = 0;
+            next_tile = blockIdx.x;  // tiles blockIdx.x, +G, +2G, ... of the alive list
             scan_done = (scan_len == 0);
             credit = 1;  // this CTA's token for the level
             min_sh = NO_LEVEL;
@@ -176,9 +239,10 @@ __global__ void __launch_bounds__(PEEL_THREADS, 2) peel_kernel(PeelArgs A) {
                 unsigned qsize = q_tail - q_head;
                 if (ld_relaxed(&ctl->err) != 0) md = M_EXIT;
                 if (!md && !scan_done && qsize < LOW_WATER) {
-                    unsigned long long t = atomicAdd(&ctl->scan_cursor[s], (unsigned long long)PEEL_THREADS);
+                    unsigned long long t = next_tile * TILE;
                     if (t < scan_len) {
                         tile_base = t;
+                        next_tile += G;
                         md = M_SCAN;
                     } else {
                         scan_done = 1;
@@ -211,40 +275,52 @@ __global__ void __launch_bounds__(PEEL_THREADS, 2) peel_kernel(PeelArgs A) {
                         atomicAdd(&ctl->pending[s], (unsigned long long)(0ull - credit));
                         credit = 0;
                     }
-                    // probe the shared queues, starting at a rotating index
+                    // Shared queues: a CTA reserves up to steal_max slots with one
+                    // atomicAdd on the queue head (never fails) and takes the
+                    // items as producers fill them.  Slots still empty when the
+                    // level's credit count reaches zero will never be filled
+                    // (producers push only while holding credit) and are dropped.
                     md = M_SPIN;
-                    bool seen = false;
-                    for (unsigned k = 0; k < A.nq && md == M_SPIN; k++) {
-                        const unsigned qi = (probe + k) % A.nq;
-                        unsigned long long h = ld_relaxed64(&ctl->q[s][qi].head);
-                        unsigned long long t = ld_relaxed64(&ctl->q[s][qi].tail);
-                        if (t > A.gq_cap) t = A.gq_cap;  // an overflow was flagged; never read past the end
-                        if (h >= t) continue;
-                        seen = true;
-                        unsigned long long take = t - h;
-                        if (take > A.steal_max) take = A.steal_max;
-                        if (atomicCAS(&ctl->q[s][qi].head, h, h + take) == h) {
-                            steal_base = ((unsigned long long)s * A.nq + qi) * A.gq_cap + h;
-                            steal_n = (unsigned)take;
-                            credit += take;
+                    if (res_mask == 0) {
+                        for (unsigned k = 0; k < A.nq; k++) {
+                            const unsigned qi = (probe + k) % A.nq;
+                            unsigned long long h = ld_relaxed64(&ctl->q[s][qi].head);
+                            unsigned long long t = ld_relaxed64(&ctl->q[s][qi].tail);
+                            if (t > A.gq_cap) t = A.gq_cap;  // an overflow was flagged; never read past the end
+                            if (h >= t) continue;
+                            unsigned long long want = (t - h + 3) / 4;
+                            if (want > A.steal_max) want = A.steal_max;
+                            unsigned long long r = atomicAdd(&ctl->q[s][qi].head, want);
+                            if (r < A.gq_cap) {
+                                if (r + want > A.gq_cap) want = A.gq_cap - r;
+                                res_base = ((unsigned long long)s * A.nq + qi) * A.gq_cap + r;
+                                res_mask = want >= 64 ? ~0ull : ((1ull << want) - 1);
+                                if (A.trace && li < A.trace_cap) atomicAdd(&A.trace[li].steals, 1u);
+                            }
+                            probe = qi;
+                            break;
+                        }
+                    }
+                    if (res_mask != 0) {
+                        const unsigned j0 = __ffsll((long long)res_mask) - 1;
+                        if (ld_relaxed64(&A.gq[res_base + j0]) != SENT) {
                             md = M_STEAL;
                             wait_t0 = 0;
-                            probe = qi;
-                            if (A.trace && li < A.trace_cap) atomicAdd(&A.trace[li].steals, 1u);
                         } else if (A.trace && li < A.trace_cap) {
                             atomicAdd(&A.trace[li].steal_fail, 1u);
                         }
                     }
-                    if (md != M_SPIN || seen) {
-                        if (md == M_SPIN) probe++;
-                    } else if (ld_acquire64(&ctl->pending[s]) == 0ull) {
-                        md = M_DONE;
-                    } else {
-                        unsigned long long now = global_ns();
-                        if (wait_t0 == 0) wait_t0 = now;
-                        else if (now - wait_t0 > A.timeout_ns) {
-                            set_err(ctl, KC_ERR_TIMEOUT, 1);
-                            md = M_EXIT;
+                    if (md == M_SPIN) {
+                        if (ld_acquire64(&ctl->pending[s]) == 0ull) {
+                            res_mask = 0;  // the level is over: nothing more will arrive
+                            md = M_DONE;
+                        } else {
+                            unsigned long long now = global_ns();
+                            if (wait_t0 == 0) wait_t0 = now;
+                            else if (now - wait_t0 > A.timeout_ns) {
+                                set_err(ctl, KC_ERR_TIMEOUT, 1);
+                                md = M_EXIT;
+                            }
                         }
                     }
                 }
@@ -261,83 +337,109 @@ __global__ void __launch_bounds__(PEEL_THREADS, 2) peel_kernel(PeelArgs A) {
             }
 
             if (md == M_STEAL) {
-                const unsigned long long base = steal_base;
-                const unsigned cnt = steal_n;
+                // take every filled slot of the reservation into the CTA queue
+                const unsigned long long mask = res_mask;
                 const unsigned qt = q_tail;
-                for (unsigned j = tid; j < cnt; j += PEEL_THREADS) {
-                    unsigned long long *slot = &A.gq[base + j];
+                if (tid < 64 && ((mask >> tid) & 1ull)) {
+                    unsigned long long *slot = &A.gq[res_base + tid];
                     unsigned long long it = ld_relaxed64(slot);
-                    unsigned long long t0 = 0;
-                    unsigned spins = 0;
-                    while (it == SENT) {
-                        if (ld_relaxed(&ctl->err) != 0) break;
-                        if ((++spins & 255u) == 0) {
-                            unsigned long long now = global_ns();
-                            if (t0 == 0) t0 = now;
-                            else if (now - t0 > A.timeout_ns) { set_err(ctl, KC_ERR_TIMEOUT, 2); break; }
-                        }
-                        __nanosleep(20);
-                        it = ld_relaxed64(slot);
+                    if (it != SENT) {
+                        st_relaxed64(slot, SENT);
+                        unsigned pos = atomicAdd(&steal_cnt, 1u);
+                        q[(qt + pos) % QCAP] = it;
+                        atomicAnd(&res_mask, ~(1ull << tid));
                     }
-                    st_relaxed64(slot, SENT);
-                    q[(qt + j) % QCAP] = it;
                 }
                 __syncthreads();
-                if (tid == 0) q_tail = qt + cnt;
+                if (tid == 0) {
+                    q_tail = qt + steal_cnt;
+                    credit += steal_cnt;
+                    steal_cnt = 0;
+                }
                 __syncthreads();
                 continue;
             }
 
             if (md == M_SCAN) {
-                // ---- scan one tile of the alive list -----------------------
-                const unsigned long long pos = tile_base + tid;
-                const bool inr = pos < scan_len;
-                uint32_t v = 0;
-                bool keep = false, take = false;
+                // ---- scan one tile (SCAN_U entries per thread) of the alive list
+                uint32_t v[SCAN_U];
+                unsigned w[SCAN_U], d[SCAN_U];
+                bool inr[SCAN_U], keep[SCAN_U], take[SCAN_U], push[SCAN_U];
+#pragma unroll
+                for (int k = 0; k < SCAN_U; k++) {
+                    const unsigned long long pos = tile_base + (unsigned)k * PEEL_THREADS + tid;
+                    inr[k] = pos < scan_len;
+                    v[k] = inr[k] ? src[pos] : 0u;
+                }
+#pragma unroll
+                for (int k = 0; k < SCAN_U; k++) w[k] = inr[k] ? __ldcg(&A.claimed[v[k] >> 5]) : 0xffffffffu;
+#pragma unroll
+                for (int k = 0; k < SCAN_U; k++) {
+                    inr[k] = inr[k] && !(w[k] & (1u << (v[k] & 31)));
+                    d[k] = inr[k] ? __ldcg(&A.deg[v[k]]) : 0u;
+                }
                 unsigned dkeep = NO_LEVEL;
-                if (inr) {
-                    v = (li == 0) ? (uint32_t)pos : src[pos];
-                    unsigned w = __ldcg(&A.claimed[v >> 5]);
-                    unsigned bit = 1u << (v & 31);
-                    if (!(w & bit)) {
-                        unsigned d = __ldcg(&A.deg[v]);
-                        if ((int)d <= (int)L) {
-                            unsigned old = atomicOr(&A.claimed[v >> 5], bit);
-                            take = !(old & bit);
-                        } else {
-                            keep = true;
-                            dkeep = d;
-                        }
-                    }
+#pragma unroll
+                for (int k = 0; k < SCAN_U; k++) {
+                    keep[k] = inr[k] && (int)d[k] > (int)L;
+                    if (keep[k]) dkeep = min(dkeep, d[k]);
+                    // claims: lanes whose vertices share a bitmap word set their
+                    // bits with one atomicOr by the lowest such lane
+                    const bool want = inr[k] && !keep[k];
+                    const unsigned word = want ? (v[k] >> 5) : 0xffffffffu;
+                    const unsigned bit = want ? (1u << (v[k] & 31)) : 0u;
+                    const unsigned peers = __match_any_sync(KC_FULL_MASK, word);
+                    const unsigned bits = __reduce_or_sync(peers, bit);
+                    const int leader = __ffs(peers) - 1;
+                    unsigned old = 0;
+                    if (want && (int)lane == leader) old = atomicOr(&A.claimed[word], bits);
+                    old = __shfl_sync(KC_FULL_MASK, old, leader);
+                    take[k] = want && !(old & bit);
                 }
                 dkeep = __reduce_min_sync(KC_FULL_MASK, dkeep);
                 if (lane == 0 && dkeep != NO_LEVEL) atomicMin(&min_sh, dkeep);
-                // a claimed vertex with an empty row needs no processing
-                const bool push = take && (A.rowptr[v + 1] != A.rowptr[v]);
-                unsigned kb = __ballot_sync(KC_FULL_MASK, keep);
-                unsigned cb = __ballot_sync(KC_FULL_MASK, push);
-                const unsigned tb = __ballot_sync(KC_FULL_MASK, take);
-                if (lane == 0 && tb != 0u) {
-                    claimed_any = 1;
-                    if (A.trace) atomicAdd(&claims_sh, (unsigned)__popc(tb));
+                unsigned kb[SCAN_U], cb[SCAN_U];
+                unsigned any_take = 0;
+#pragma unroll
+                for (int k = 0; k < SCAN_U; k++) {
+                    // a claimed vertex with an empty row needs no processing
+                    push[k] = take[k] && (A.rowptr[v[k] + 1] != A.rowptr[v[k]]);
+                    kb[k] = __ballot_sync(KC_FULL_MASK, keep[k]);
+                    cb[k] = __ballot_sync(KC_FULL_MASK, push[k]);
+                    const unsigned tb = __ballot_sync(KC_FULL_MASK, take[k]);
+                    any_take += __popc(tb);
+                    if (lane == 0) warp_cnt[k][warp] = __popc(kb[k]) | (__popc(cb[k]) << 16);
                 }
-                if (lane == 0) warp_cnt[warp] = __popc(kb) | (__popc(cb) << 16);
+                if (lane == 0 && any_take) {
+                    claimed_any = 1;
+                    if (A.trace) atomicAdd(&claims_sh, any_take);
+                }
                 __syncthreads();
-                unsigned kofs = 0, cofs = 0, ktot = 0, ctot = 0;
-                for (unsigned w2 = 0; w2 < PEEL_WARPS; w2++) {
-                    unsigned x = warp_cnt[w2];
-                    if (w2 < warp) {
-                        kofs += x & 0xffffu;
-                        cofs += x >> 16;
+                // offsets: sub-tiles in order, warps in order within a sub-tile
+                unsigned ktot = 0, ctot = 0;
+                unsigned kofs[SCAN_U], cofs[SCAN_U];
+#pragma unroll
+                for (int k = 0; k < SCAN_U; k++) {
+                    kofs[k] = ktot;
+                    cofs[k] = ctot;
+                    for (unsigned w2 = 0; w2 < PEEL_WARPS; w2++) {
+                        unsigned x = warp_cnt[k][w2];
+                        if (w2 < warp) {
+                            kofs[k] += x & 0xffffu;
+                            cofs[k] += x >> 16;
+                        }
+                        ktot += x & 0xffffu;
+                        ctot += x >> 16;
                     }
-                    ktot += x & 0xffffu;
-                    ctot += x >> 16;
                 }
                 if (tid == 0 && ktot) out_base = atomicAdd(&ctl->out_len[s], (unsigned long long)ktot);
                 __syncthreads();
                 const unsigned lt = (1u << lane) - 1u;
-                if (keep) dst[out_base + kofs + __popc(kb & lt)] = v;
-                if (push) q[(q_tail + cofs + __popc(cb & lt)) % QCAP] = ((unsigned long long)v << 32);
+#pragma unroll
+                for (int k = 0; k < SCAN_U; k++) {
+                    if (keep[k]) dst[out_base + kofs[k] + __popc(kb[k] & lt)] = v[k];
+                    if (push[k]) q[(q_tail + cofs[k] + __popc(cb[k] & lt)) % QCAP] = ((unsigned long long)v[k] << 32);
+                }
                 __syncthreads();
                 if (tid == 0) q_tail += ctot;
                 __syncthreads();
@@ -611,7 +713,8 @@ int peel_run(Graph *g, cudaStream_t s, bool gpp_zero_to_one_flag, kc_stats *st) 
     KC_CUDA(cudaEventRecord(g->ev0, s));
     if (A.trace) KC_CUDA(cudaMemsetAsync(g->trace, 0, sizeof(PeelTrace) * g->trace_cap, s));
     const int ig = std::max(1, std::min<int>(g->sm_count * 8, (int)((g->n + 255) / 256)));
-    peel_init<<<ig, 256, 0, s>>>(g->rowptr, g->n, g->core, g->bitmap, g->peel_ctl, (unsigned)grid);
+    peel_ctl_reset<<<1, 1, 0, s>>>(g->peel_ctl, (unsigned)grid);
+    peel_init<<<ig, 256, 0, s>>>(g->rowptr, g->n, g->core, g->bitmap, g->alive + g->n, g->peel_ctl, (unsigned)grid);
     void *args[] = {&A};
     KC_CUDA(cudaEventRecord(g->evk0, s));
     KC_CUDA(cudaLaunchCooperativeKernel((const void *)peel_kernel, dim3(grid), dim3(PEEL_THREADS), args, 0, s));

@@ -208,3 +208,17 @@ def test_config2_rmat22_ef16():
         got, st = g.decompose(m)
         assert np.array_equal(got, core), m
         assert st.kmax == kmax
+
+
+def test_config3_rmat25_planted_core():
+    """R-MAT scale 25, edge factor 16, plus a planted 4000-vertex subgraph at
+    p = 0.6: bit-exact against Batagelj-Zaversnik at full size."""
+    g = pg.rmat_planted_graph(25, 16, 4000, 0.6, seed=3)
+    assert g.n == 1 << 25 and g.nnz > 1_000_000_000
+    got, st = g.decompose("peelone_dyn")
+    rp, col = g.csr()
+    core, kmax = oracle.bz(rp, col)
+    assert np.array_equal(got, core)
+    assert st.kmax == kmax and kmax >= 2000  # the planted core dominates
+    got_h, _ = g.decompose("NbrCore")
+    assert np.array_equal(got_h, core)

@@ -15,7 +15,7 @@ SETTINGS = [
     {"peel.queues": 64, "peel.steal": 1},
     {"peel.spill": 0, "peel.steal": 3},
     {"peel.spill": 0, "peel.queues": 7, "peel.chunk": 256},
-    {"peel.spill": 3072, "peel.steal": 2048, "peel.chunk": 65536},
+    {"peel.spill": 3072, "peel.steal": 64, "peel.chunk": 65536},
     {"peel.ctas_per_sm": 1, "peel.queues": 32},
     {"peel.chunk": 256, "peel.steal": 5, "peel.queues": 3},
 ]
