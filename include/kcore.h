@@ -195,6 +195,37 @@ int kc_graph_trace(const kc_graph *g, kc_level_trace *out, uint32_t cap, uint32_
 /* Device pointer of the last decomposition's core array (n uint32). */
 int kc_graph_device_core(const kc_graph *g, const uint32_t **d_core);
 
+/* ---- batched decomposition -------------------------------------------- */
+/* Many independent graphs decomposed together.  The graphs are packed into
+ * one kc_graph (a segmented CSR): graph i owns vertices [vbase[i],
+ * vbase[i+1]) and its rows reference only its own vertices (checked at
+ * creation).  The reference decomposes one graph per program run; the plain
+ * equivalent here is one kc_decompose per graph (see kc_graph_from_segment).
+ * A kc_batch holds the plan (size classes, work lists, tuning, captured CUDA
+ * graph) and uses the kc_graph's core array for its results. */
+typedef struct kc_batch kc_batch;
+int kc_batch_create(kc_graph *g, const uint32_t *vbase, uint32_t num_graphs, kc_batch **out);
+/* Parameters: "batch.small_n" (largest graph, in vertices, of the small-CTA
+ * class), "batch.small_threads", "batch.large_threads", "batch.chunk" (row
+ * entries per work item), "batch.cuda_graph" (1 = capture once, replay),
+ * "trace" (1 = record per-graph timings, see kc_batch_trace). */
+int kc_batch_set_param(kc_batch *b, const char *name, int64_t value);
+int kc_batch_get_param(const kc_batch *b, const char *name, int64_t *value);
+/* Times a grid of configurations on this batch and keeps the fastest;
+ * *best_ms receives its time. */
+int kc_batch_autotune(kc_batch *b, double *best_ms);
+/* Core numbers of every packed vertex (n uint32, host or device buffer; NULL
+ * keeps them in the graph's core array).  stats->ms = device time. */
+int kc_batch_decompose(kc_batch *b, uint32_t *core_out, int out_on_device, kc_stats *stats, void *stream);
+/* With parameter "trace" = 1, each decomposition records per graph i the GPU
+ * timer at its start and end and the SM that ran it: out[3i], out[3i+1],
+ * out[3i+2] (cap = number of uint64 slots of out). */
+int kc_batch_trace(const kc_batch *b, uint64_t *out, uint32_t cap);
+int kc_batch_free(kc_batch *b);
+/* A standalone graph made of vertices [lo, hi) of g, ids rebased to 0; the
+ * rows of those vertices must reference only [lo, hi). */
+int kc_graph_from_segment(const kc_graph *g, uint32_t lo, uint32_t hi, kc_graph **out);
+
 /* ---- memory helpers ----------------------------------------------------
  * The reference allocates and copies inside each driver
  * (peel/src/gpu_memory_allocation.cu:4-21, HistoCore.cu:259-286); callers of
@@ -227,6 +258,18 @@ int kc_gen_er(uint32_t n, uint64_t m, uint64_t seed, uint32_t *d_src, uint32_t *
  * most cap edges; *m receives the count (KC_ERR_CAPACITY if cap is short). */
 int kc_gen_planted(uint32_t n, uint32_t k, double p, uint64_t seed, uint32_t *d_src, uint32_t *d_dst,
                    uint64_t cap, uint64_t *m, void *stream);
+
+/* R-MAT over [0, n) for any n >= 2: 2^ceil(log2 n) ids, draws with an
+ * endpoint >= n are rejected and written as the self-loop (0, 0). */
+int kc_gen_rmat_bounded(uint32_t n, uint64_t num_edges, double a, double b, double c, uint64_t seed,
+                        uint32_t *d_src, uint32_t *d_dst, void *stream);
+/* Barabasi-Albert preferential attachment: n vertices, d edges per vertex
+ * (n*d edges; vertex v creates edges v*d .. v*d+d-1 towards endpoints of
+ * earlier edges), in the copy-model formulation of Batagelj and Brandes. */
+int kc_gen_ba(uint32_t n, uint32_t d, uint64_t seed, uint32_t *d_src, uint32_t *d_dst, void *stream);
+/* Add `offset` to every endpoint of a device edge list (packing graphs into
+ * one id space). */
+int kc_edges_offset(uint32_t *d_src, uint32_t *d_dst, uint64_t m, uint32_t offset, void *stream);
 
 #ifdef __cplusplus
 }

@@ -129,3 +129,35 @@ def planted(n, k, prob, seed):
     sel = p[h < np.uint64(_thr(prob))]
     a, b = tri_unrank(k, sel)
     return members[a.astype(np.int64)], members[b.astype(np.int64)]
+
+
+def ba(n, d, seed):
+    """Barabasi-Albert edge list of pico_gb300/csrc/gen.cu (Batagelj-Brandes
+    copy model, each odd slot resolved by following r = hash(slot) % slot)."""
+    m = n * d
+    k = np.arange(m, dtype=np.uint64)
+    slot = 2 * k + np.uint64(1)
+    target = np.zeros(m, dtype=np.uint64)
+    todo = np.ones(m, dtype=bool)
+    for _ in range(4096):
+        if not todo.any():
+            break
+        with np.errstate(over="ignore"):
+            r = mix64(np.uint64(seed) * np.uint64(0x9FB21C651E98DF25) + slot[todo]) % slot[todo]
+        even = (r & np.uint64(1)) == 0
+        idx = np.flatnonzero(todo)
+        target[idx[even]] = (r[even] >> np.uint64(1)) // np.uint64(d)
+        slot[idx[~even]] = r[~even]
+        todo[idx[even]] = False
+    return (k // np.uint64(d)).astype(np.uint32), target.astype(np.uint32)
+
+
+def rmat_bounded(n, m, seed, a=0.57, b=0.19, c=0.19):
+    scale = 1
+    while (1 << scale) < n:
+        scale += 1
+    u, v = rmat_numpy(scale, m, seed, a, b, c)
+    bad = (u >= n) | (v >= n)
+    u[bad] = 0
+    v[bad] = 0
+    return u, v

@@ -125,6 +125,17 @@ def lib():
     _sig(L, "kc_gen_rmat", i, [u32, u64, d, d, d, u64, _P, _P, _P])
     _sig(L, "kc_gen_er", i, [u32, u64, u64, _P, _P, _P])
     _sig(L, "kc_gen_planted", i, [u32, u32, d, u64, _P, _P, u64, _U64P, _P])
+    _sig(L, "kc_gen_rmat_bounded", i, [u32, u64, d, d, d, u64, _P, _P, _P])
+    _sig(L, "kc_gen_ba", i, [u32, u32, u64, _P, _P, _P])
+    _sig(L, "kc_edges_offset", i, [_P, _P, u64, u32, _P])
+    _sig(L, "kc_batch_create", i, [_P, _P, u32, PP])
+    _sig(L, "kc_batch_set_param", i, [_P, ctypes.c_char_p, ctypes.c_int64])
+    _sig(L, "kc_batch_get_param", i, [_P, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int64)])
+    _sig(L, "kc_batch_autotune", i, [_P, ctypes.POINTER(ctypes.c_double)])
+    _sig(L, "kc_batch_decompose", i, [_P, _P, i, ctypes.POINTER(kc_stats), _P])
+    _sig(L, "kc_batch_free", i, [_P])
+    _sig(L, "kc_batch_trace", i, [_P, _P, u32])
+    _sig(L, "kc_graph_from_segment", i, [_P, u32, u32, PP])
     _lib = L
     return L
 
@@ -344,6 +355,12 @@ class Graph:
         keys = [f[0] for f in kc_level_trace._fields_]
         return [{k: getattr(buf[i], k) for k in keys} for i in range(cnt.value)]
 
+    def segment(self, lo, hi):
+        """Standalone graph of vertices [lo, hi) (ids rebased to 0)."""
+        h = ctypes.c_void_p()
+        check(lib().kc_graph_from_segment(self._h, int(lo), int(hi), ctypes.byref(h)))
+        return Graph(h.value, self.device)
+
     def device_core(self):
         p = ctypes.c_void_p()
         check(lib().kc_graph_device_core(self._h, ctypes.byref(p)))
@@ -441,3 +458,59 @@ def rmat_planted_graph(scale, edge_factor, k, p, seed, abc=RMAT_ABC, device=0):
     s.free()
     d.free()
     return g
+
+
+class Batch:
+    """Batched decomposition of the graphs packed in `graph` (segments vbase)."""
+
+    def __init__(self, graph, vbase):
+        self.graph = graph
+        self.vbase = np.ascontiguousarray(vbase, dtype=np.uint32)
+        h = ctypes.c_void_p()
+        check(lib().kc_batch_create(graph.handle, _ptr(self.vbase), self.vbase.size - 1, ctypes.byref(h)))
+        self._h = h
+
+    @property
+    def num_graphs(self):
+        return self.vbase.size - 1
+
+    def set_param(self, name, value):
+        check(lib().kc_batch_set_param(self._h, name.encode(), int(value)))
+
+    def get_param(self, name):
+        v = ctypes.c_int64()
+        check(lib().kc_batch_get_param(self._h, name.encode(), ctypes.byref(v)))
+        return v.value
+
+    def autotune(self):
+        t = ctypes.c_double()
+        check(lib().kc_batch_autotune(self._h, ctypes.byref(t)))
+        return t.value
+
+    def decompose(self, out=None, stream=0):
+        core = out if out is not None else np.empty(max(self.graph.n, 1), dtype=np.uint32)
+        st = kc_stats()
+        check(lib().kc_batch_decompose(self._h, _ptr(core), 0, ctypes.byref(st), ctypes.c_void_p(stream)))
+        return core[:self.graph.n], st.ms
+
+    def decompose_device(self, stream=0):
+        st = kc_stats()
+        check(lib().kc_batch_decompose(self._h, None, 0, ctypes.byref(st), ctypes.c_void_p(stream)))
+        return st.ms
+
+    def trace(self):
+        """(start_ns, end_ns, sm) per graph of the last decomposition (after set_param("trace", 1))."""
+        out = np.zeros(3 * self.num_graphs, dtype=np.uint64)
+        check(lib().kc_batch_trace(self._h, _ptr(out), out.size))
+        return out.reshape(-1, 3)
+
+    def free(self):
+        if self._h is not None and self._h.value:
+            lib().kc_batch_free(self._h)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass

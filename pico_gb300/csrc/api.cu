@@ -249,6 +249,41 @@ int kc_graph_from_csr_device(const int64_t *d_rowptr, const uint32_t *d_col, uin
     return from_csr_common(d_rowptr, d_col, n, device, out, cudaMemcpyDeviceToDevice);
 }
 
+__global__ void segment_rebase(const int64_t *__restrict__ rowptr, const uint32_t *__restrict__ col, uint32_t lo,
+                               uint32_t n, int64_t *nrow, uint32_t *ncol) {
+    const int64_t base = rowptr[lo];
+    const int64_t nnz = rowptr[lo + n] - base;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v <= n; v += stride) nrow[v] = rowptr[lo + v] - base;
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < (uint64_t)nnz; e += stride)
+        ncol[e] = col[base + e] - lo;
+}
+
+int kc_graph_from_segment(const kc_graph *g, uint32_t lo, uint32_t hi, kc_graph **out) {
+    clear_error();
+    if (!g || !out || hi < lo || hi > g->n) return fail(KC_ERR_INVALID, "bad segment");
+    *out = nullptr;
+    kc_graph *h = nullptr;
+    KC_TRY(new_graph(g->device, &h));
+    h->n = hi - lo;
+    int64_t r[2];
+    cudaMemcpy(&r[0], g->rowptr + lo, 8, cudaMemcpyDeviceToHost);
+    cudaMemcpy(&r[1], g->rowptr + hi, 8, cudaMemcpyDeviceToHost);
+    h->nnz = (uint64_t)(r[1] - r[0]);
+    int rc = dalloc(&h->rowptr, (uint64_t)h->n + 1, "row offsets");
+    if (!rc) rc = dalloc(&h->col, h->nnz + 1, "column ids");
+    if (rc) { delete h; return rc; }
+    const uint64_t items = std::max<uint64_t>(h->nnz, (uint64_t)h->n + 1);
+    const int blocks = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)h->sm_count * 8, (items + 255) / 256));
+    segment_rebase<<<blocks, 256, 0, h->stream>>>(g->rowptr, g->col, lo, h->n, h->rowptr, h->col);
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) { delete h; return fail(KC_ERR_CUDA, "segment: %s", cudaGetErrorString(e)); }
+    rc = graph_finish(h);
+    if (rc) { delete h; return rc; }
+    *out = h;
+    return KC_OK;
+}
+
 int kc_graph_validate(kc_graph *g, uint64_t *bad) {
     clear_error();
     if (!g || !bad) return fail(KC_ERR_INVALID, "null argument");
@@ -489,6 +524,22 @@ int kc_gen_planted(uint32_t n, uint32_t k, double p, uint64_t seed, uint32_t *d_
     clear_error();
     if (!m) return fail(KC_ERR_INVALID, "null argument");
     return gen_planted(n, k, p, seed, d_src, d_dst, cap, m, static_cast<cudaStream_t>(stream));
+}
+
+int kc_gen_rmat_bounded(uint32_t n, uint64_t num_edges, double a, double b, double c, uint64_t seed, uint32_t *d_src,
+                        uint32_t *d_dst, void *stream) {
+    clear_error();
+    return gen_rmat_bounded(n, num_edges, a, b, c, seed, d_src, d_dst, static_cast<cudaStream_t>(stream));
+}
+
+int kc_gen_ba(uint32_t n, uint32_t d, uint64_t seed, uint32_t *d_src, uint32_t *d_dst, void *stream) {
+    clear_error();
+    return gen_ba(n, d, seed, d_src, d_dst, static_cast<cudaStream_t>(stream));
+}
+
+int kc_edges_offset(uint32_t *d_src, uint32_t *d_dst, uint64_t m, uint32_t offset, void *stream) {
+    clear_error();
+    return edges_offset(d_src, d_dst, m, offset, static_cast<cudaStream_t>(stream));
 }
 
 }  // extern "C"

@@ -216,3 +216,97 @@ int gen_planted(uint32_t n, uint32_t k, double p, uint64_t seed, uint32_t *d_src
 }
 
 }  // namespace kc
+
+namespace kc {
+
+// ------------------------------------------------ bounded R-MAT / offsets --
+// R-MAT over 2^ceil(log2 n) ids with draws outside [0, n) rejected: a
+// rejected draw is written as the self-loop (0, 0), which the CSR build drops.
+__global__ void rmat_bounded_kernel(uint32_t scale, uint32_t n, uint64_t m, uint64_t ta, uint64_t tab, uint64_t tabc,
+                                    uint64_t seed, uint32_t *src, uint32_t *dst) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < m; i += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t base = mix64(seed * 0xD1B54A32D192ED03ull + i);
+        uint32_t u = 0, v = 0;
+        uint64_t word = 0;
+        for (uint32_t b = 0; b < scale; b++) {
+            if ((b & 1) == 0) word = mix64(base ^ ((uint64_t)((b >> 1) + 1) * 0xA24BAED4963EE407ull));
+            uint32_t r = (uint32_t)(word >> (32 * (b & 1)));
+            uint32_t q = r < ta ? 0u : (r < tab ? 1u : (r < tabc ? 2u : 3u));
+            u = (u << 1) | (q >> 1);
+            v = (v << 1) | (q & 1u);
+        }
+        if (u >= n || v >= n) u = v = 0;
+        src[i] = u;
+        dst[i] = v;
+    }
+}
+
+int gen_rmat_bounded(uint32_t n, uint64_t num_edges, double a, double b, double c, uint64_t seed, uint32_t *d_src,
+                     uint32_t *d_dst, cudaStream_t s) {
+    if (n < 2) return fail(KC_ERR_INVALID, "bounded R-MAT needs n >= 2");
+    uint32_t scale = 1;
+    while (scale < 32 && (1ull << scale) < n) scale++;
+    if (a < 0 || b < 0 || c < 0 || a + b + c > 1.0) return fail(KC_ERR_INVALID, "R-MAT probabilities invalid");
+    if (!num_edges) return KC_OK;
+    uint64_t blocks = (num_edges + 255) / 256;
+    if (blocks > 65535ull * 16) blocks = 65535ull * 16;
+    rmat_bounded_kernel<<<(unsigned)blocks, 256, 0, s>>>(scale, n, num_edges, prob_threshold(a), prob_threshold(a + b),
+                                                         prob_threshold(a + b + c), seed, d_src, d_dst);
+    KC_CUDA(cudaGetLastError());
+    return KC_OK;
+}
+
+// ----------------------------------------------------- Barabasi-Albert ----
+// Batagelj and Brandes' linear-time formulation ("Efficient generation of
+// large random networks", Phys. Rev. E 71, 2005): an array M of 2*n*d slots
+// where M[2k] = k / d is the vertex that created edge k and M[2k+1] = M[r]
+// for r uniform in [0, 2k+1) -- choosing an endpoint of an earlier edge is
+// choosing a vertex with probability proportional to its degree.  Each odd
+// slot is resolved independently by following r back until it lands on an
+// even slot (expected O(log) steps), with r drawn from a counter hash, so the
+// whole array is generated in parallel.  Edge k = (k / d, M[2k+1]).
+__global__ void ba_kernel(uint32_t n, uint32_t d, uint64_t seed, uint32_t *src, uint32_t *dst) {
+    const uint64_t m = (uint64_t)n * d;
+    for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < m; k += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t slot = 2 * k + 1;
+        uint32_t target = 0;
+        for (int guard = 0; guard < 4096; guard++) {
+            uint64_t r = mix64(seed * 0x9FB21C651E98DF25ull + slot) % slot;
+            if ((r & 1) == 0) {
+                target = (uint32_t)((r >> 1) / d);
+                break;
+            }
+            slot = r;
+        }
+        src[k] = (uint32_t)(k / d);
+        dst[k] = target;
+    }
+}
+
+int gen_ba(uint32_t n, uint32_t d, uint64_t seed, uint32_t *d_src, uint32_t *d_dst, cudaStream_t s) {
+    if (n < 1 || d < 1) return fail(KC_ERR_INVALID, "Barabasi-Albert needs n >= 1 and d >= 1");
+    uint64_t m = (uint64_t)n * d;
+    uint64_t blocks = (m + 255) / 256;
+    if (blocks > 65535ull * 16) blocks = 65535ull * 16;
+    ba_kernel<<<(unsigned)blocks, 256, 0, s>>>(n, d, seed, d_src, d_dst);
+    KC_CUDA(cudaGetLastError());
+    return KC_OK;
+}
+
+__global__ void offset_kernel(uint32_t *src, uint32_t *dst, uint64_t m, uint32_t off) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < m; i += (uint64_t)gridDim.x * blockDim.x) {
+        src[i] += off;
+        dst[i] += off;
+    }
+}
+
+int edges_offset(uint32_t *d_src, uint32_t *d_dst, uint64_t m, uint32_t off, cudaStream_t s) {
+    if (!m || !off) return KC_OK;
+    uint64_t blocks = (m + 255) / 256;
+    if (blocks > 65535ull * 16) blocks = 65535ull * 16;
+    offset_kernel<<<(unsigned)blocks, 256, 0, s>>>(d_src, d_dst, m, off);
+    KC_CUDA(cudaGetLastError());
+    return KC_OK;
+}
+
+}  // namespace kc

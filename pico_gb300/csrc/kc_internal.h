@@ -154,6 +154,10 @@ int gen_rmat(uint32_t scale, uint64_t num_edges, double a, double b, double c, u
 int gen_er(uint32_t n, uint64_t m, uint64_t seed, uint32_t *d_src, uint32_t *d_dst, cudaStream_t s);
 int gen_planted(uint32_t n, uint32_t k, double p, uint64_t seed, uint32_t *d_src, uint32_t *d_dst,
                 uint64_t cap, uint64_t *m, cudaStream_t s);
+int gen_rmat_bounded(uint32_t n, uint64_t num_edges, double a, double b, double c, uint64_t seed, uint32_t *d_src,
+                     uint32_t *d_dst, cudaStream_t s);
+int gen_ba(uint32_t n, uint32_t d, uint64_t seed, uint32_t *d_src, uint32_t *d_dst, cudaStream_t s);
+int edges_offset(uint32_t *d_src, uint32_t *d_dst, uint64_t m, uint32_t off, cudaStream_t s);
 
 }  // namespace kc
 
