@@ -176,7 +176,9 @@ int kc_graph_last_timing(const kc_graph *g, double *total_ms, double *kernel_ms)
  * item), "peel.spill" (cascade items a CTA keeps before publishing to the
  * shared queues), "peel.steal" (most items reserved per steal, 1..64), "peel.queues" (number
  * of shared queues, 1..64), "peel.ctas_per_sm" (0 = occupancy maximum),
- * "trace" (1 = record a per-level trace of the next decompositions). */
+ * "trace" (1 = record a per-level trace of the next decompositions),
+ * "update.incremental_max" (largest update batch, in edges, maintained
+ * incrementally by kc_graph_update). */
 int kc_graph_set_param(kc_graph *g, const char *name, int64_t value);
 
 /* Per-level trace of the last peel decomposition (recorded when the "trace"
@@ -194,6 +196,31 @@ int kc_graph_trace(const kc_graph *g, kc_level_trace *out, uint32_t cap, uint32_
 
 /* Device pointer of the last decomposition's core array (n uint32). */
 int kc_graph_device_core(const kc_graph *g, const uint32_t **d_core);
+
+/* ---- dynamic graphs: exact core maintenance under edge batches ---------- */
+/* No counterpart in the reference (its "dyn" drivers use dynamic work
+ * queues, not edge updates).  Applies a batch to a graph built with
+ * KC_EDGES_DEDUP (sorted rows, no parallel edges) and keeps the core numbers
+ * exact: deletions first, then insertions; deleting an absent edge or
+ * inserting a present one is ignored; self-loops are ignored.  Batches of at
+ * most "update.incremental_max" edges (kc_graph_set_param) are maintained
+ * incrementally (h-index iteration from the old cores for deletions;
+ * matching rounds with subcore candidate sets for insertions); larger ones
+ * are applied in one rewrite followed by a full decomposition.  Edge lists in
+ * host memory; core_out as in kc_decompose (may be NULL). */
+typedef struct kc_update_stats {
+    uint64_t inserted;    /* undirected edges added */
+    uint64_t deleted;     /* undirected edges removed */
+    uint32_t rounds;      /* insertion matchings processed */
+    uint32_t sweeps;      /* h-index sweeps, summed */
+    uint64_t candidates;  /* vertices re-examined after insertions */
+    uint32_t recomputed;  /* 1 = applied through a full decomposition */
+    uint32_t reserved;
+    double ms;            /* wall time of the call */
+} kc_update_stats;
+int kc_graph_update(kc_graph *g, const uint32_t *ins_src, const uint32_t *ins_dst, uint64_t n_ins,
+                    const uint32_t *del_src, const uint32_t *del_dst, uint64_t n_del, uint32_t *core_out,
+                    int out_on_device, kc_update_stats *stats);
 
 /* ---- batched decomposition -------------------------------------------- */
 /* Many independent graphs decomposed together.  The graphs are packed into

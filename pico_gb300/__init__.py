@@ -52,6 +52,12 @@ class kc_stats(ctypes.Structure):
                 ("build_ms", ctypes.c_double)]
 
 
+class kc_update_stats(ctypes.Structure):
+    _fields_ = [("inserted", ctypes.c_uint64), ("deleted", ctypes.c_uint64), ("rounds", ctypes.c_uint32),
+                ("sweeps", ctypes.c_uint32), ("candidates", ctypes.c_uint64), ("recomputed", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32), ("ms", ctypes.c_double)]
+
+
 class kc_level_trace(ctypes.Structure):
     _fields_ = [("t_start_ns", ctypes.c_uint64), ("level", ctypes.c_uint32), ("claimed", ctypes.c_uint32),
                 ("scan_len", ctypes.c_uint32), ("spilled", ctypes.c_uint32), ("steals", ctypes.c_uint32),
@@ -136,6 +142,7 @@ def lib():
     _sig(L, "kc_batch_free", i, [_P])
     _sig(L, "kc_batch_trace", i, [_P, _P, u32])
     _sig(L, "kc_graph_from_segment", i, [_P, u32, u32, PP])
+    _sig(L, "kc_graph_update", i, [_P, _P, _P, u64, _P, _P, u64, _P, i, ctypes.POINTER(kc_update_stats)])
     _lib = L
     return L
 
@@ -354,6 +361,22 @@ class Graph:
         check(lib().kc_graph_trace(self._h, buf, cnt.value, ctypes.byref(cnt)))
         keys = [f[0] for f in kc_level_trace._fields_]
         return [{k: getattr(buf[i], k) for k in keys} for i in range(cnt.value)]
+
+    def update(self, ins=None, dels=None, want_core=True):
+        """Apply an edge batch (deletions first) keeping the core numbers
+        exact.  ins / dels: (src, dst) arrays.  Returns (core or None, stats dict)."""
+        e = np.zeros(0, dtype=np.uint32)
+        is_, id_ = (np.ascontiguousarray(x, dtype=np.uint32) for x in (ins if ins is not None else (e, e)))
+        ds_, dd_ = (np.ascontiguousarray(x, dtype=np.uint32) for x in (dels if dels is not None else (e, e)))
+        core = np.empty(max(self.n, 1), dtype=np.uint32) if want_core else None
+        st = kc_update_stats()
+        check(lib().kc_graph_update(self._h, _ptr(is_), _ptr(id_), is_.size, _ptr(ds_), _ptr(dd_), ds_.size,
+                                    _ptr(core) if want_core else None, 0, ctypes.byref(st)))
+        n, nnz, md, vn = ctypes.c_uint32(), ctypes.c_uint64(), ctypes.c_uint32(), ctypes.c_uint64()
+        check(lib().kc_graph_info(self._h, ctypes.byref(n), ctypes.byref(nnz), ctypes.byref(md), ctypes.byref(vn)))
+        self.nnz, self.max_degree, self.num_vnodes = nnz.value, md.value, vn.value
+        stats = {k: getattr(st, k) for k, _ in kc_update_stats._fields_ if k != "reserved"}
+        return (core[:self.n] if want_core else None), stats
 
     def segment(self, lo, hi):
         """Standalone graph of vertices [lo, hi) (ids rebased to 0)."""

@@ -57,6 +57,11 @@ Graph::~Graph() {
     dfree(hctl);
     dfree(red);
     dfree(trace);
+    dfree(mfront[0]);
+    dfree(mfront[1]);
+    dfree(mcand);
+    dfree(mvisit);
+    dfree(mcount);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
     if (evk0) cudaEventDestroy(evk0);
@@ -424,6 +429,9 @@ int kc_graph_set_param(kc_graph *g, const char *name, int64_t value) {
         t.peel_ctas_per_sm = (int)value;
     } else if (k == "trace") {
         t.trace = value ? 1 : 0;
+    } else if (k == "update.incremental_max") {
+        if (value < 0) return fail(KC_ERR_INVALID, "update.incremental_max: >= 0");
+        t.update_incremental_max = value;
     } else {
         return fail(KC_ERR_INVALID, "unknown parameter %s", name);
     }
@@ -448,6 +456,26 @@ int kc_graph_last_timing(const kc_graph *g, double *total_ms, double *kernel_ms)
     if (!g) return fail(KC_ERR_INVALID, "null graph");
     if (total_ms) *total_ms = g->last_ms;
     if (kernel_ms) *kernel_ms = g->last_kernel_ms;
+    return KC_OK;
+}
+
+int kc_graph_update(kc_graph *g, const uint32_t *ins_src, const uint32_t *ins_dst, uint64_t n_ins,
+                    const uint32_t *del_src, const uint32_t *del_dst, uint64_t n_del, uint32_t *core_out,
+                    int out_on_device, kc_update_stats *stats) {
+    clear_error();
+    if (!g || (n_ins && (!ins_src || !ins_dst)) || (n_del && (!del_src || !del_dst)))
+        return fail(KC_ERR_INVALID, "null argument");
+    KC_CUDA(cudaSetDevice(g->device));
+    int rc = graph_update(g, ins_src, ins_dst, n_ins, del_src, del_dst, n_del, stats);
+    if (rc) {
+        g->core_valid = false;
+        return rc;
+    }
+    if (core_out && g->n) {
+        KC_CUDA(cudaMemcpyAsync(core_out, g->core, (uint64_t)g->n * 4,
+                                out_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, g->stream));
+        KC_CUDA(cudaStreamSynchronize(g->stream));
+    }
     return KC_OK;
 }
 

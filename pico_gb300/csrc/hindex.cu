@@ -46,6 +46,7 @@ struct HxArgs {
     HindexCtl *ctl;
     unsigned long long timeout_ns;
     uint32_t max_sweeps;
+    uint32_t first_all;  // sweep 0 covers every vertex (else list[0] / big[0])
 };
 
 __global__ void hindex_init(const int64_t *__restrict__ rowptr, uint32_t n, uint32_t *c, uint32_t *inlist,
@@ -275,19 +276,20 @@ __global__ void __launch_bounds__(HX_THREADS, 2) hindex_kernel(HxArgs A) {
             __syncthreads();
             if (i >= nbig) break;
             uint32_t v = A.big[cur][i];
-            if (sweep > 0 && threadIdx.x == 0) atomicAnd(&A.inlist[v >> 5], ~(1u << (v & 31)));
+            if (!(sweep == 0 && A.first_all) && threadIdx.x == 0) atomicAnd(&A.inlist[v >> 5], ~(1u << (v & 31)));
             __syncthreads();
             if (hx_block_vertex(A, v, nxt, hist, red) && threadIdx.x == 0) changed_sh = 1;
             __syncthreads();
         }
         // the rest: one warp per vertex; sweep 0 covers every vertex
-        const unsigned long long nsmall = sweep == 0 ? (unsigned long long)A.n : ld_relaxed64(&ctl->list_len[cur]);
+        const bool all = sweep == 0 && A.first_all;
+        const unsigned long long nsmall = all ? (unsigned long long)A.n : ld_relaxed64(&ctl->list_len[cur]);
         uint32_t *wh = hist + warp * (HX_WARP_MAX + 1);
         bool wchanged = false;
         for (unsigned long long i = (unsigned long long)blockIdx.x * HX_WARPS + warp; i < nsmall;
              i += (unsigned long long)G * HX_WARPS) {
-            uint32_t v = sweep == 0 ? (uint32_t)i : A.list[cur][i];
-            if (sweep == 0) {
+            uint32_t v = all ? (uint32_t)i : A.list[cur][i];
+            if (all) {
                 if (A.rowptr[v + 1] - A.rowptr[v] > (int64_t)HX_WARP_MAX) continue;
             } else if (lane == 0) {
                 atomicAnd(&A.inlist[v >> 5], ~(1u << (v & 31)));
@@ -334,8 +336,7 @@ static int ensure_hx_buffers(Graph *g) {
     return KC_OK;
 }
 
-int hindex_run(Graph *g, cudaStream_t s, kc_stats *st) {
-    KC_TRY(ensure_hx_buffers(g));
+static int hindex_launch(Graph *g, cudaStream_t s, kc_stats *st, bool first_all) {
     int coop = 0;
     cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, g->device);
     if (!coop) return fail(KC_ERR_UNSUPPORTED, "device lacks cooperative launch");
@@ -343,12 +344,6 @@ int hindex_run(Graph *g, cudaStream_t s, kc_stats *st) {
     KC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, hindex_kernel, HX_THREADS, 0));
     if (occ < 1) return fail(KC_ERR_UNSUPPORTED, "h-index kernel cannot be resident");
     const int grid = occ * g->sm_count;
-    if (!g->ev0) {
-        KC_CUDA(cudaEventCreate(&g->ev0));
-        KC_CUDA(cudaEventCreate(&g->ev1));
-        KC_CUDA(cudaEventCreate(&g->evk0));
-        KC_CUDA(cudaEventCreate(&g->evk1));
-    }
     HxArgs A;
     A.rowptr = g->rowptr;
     A.col = g->col;
@@ -362,10 +357,7 @@ int hindex_run(Graph *g, cudaStream_t s, kc_stats *st) {
     A.ctl = g->hctl;
     A.timeout_ns = 20ull * 1000 * 1000 * 1000;
     A.max_sweeps = g->n + 3;  // a path needs O(n) sweeps
-    KC_CUDA(cudaEventRecord(g->ev0, s));
-    KC_CUDA(cudaMemsetAsync(g->hctl, 0, sizeof(HindexCtl), s));
-    const int ig = std::max(1, std::min<int>(g->sm_count * 8, (int)((g->n + 255) / 256)));
-    hindex_init<<<ig, 256, 0, s>>>(g->rowptr, g->n, g->core, g->bitmap, g->big[0], g->hctl);
+    A.first_all = first_all ? 1u : 0u;
     void *args[] = {&A};
     KC_CUDA(cudaEventRecord(g->evk0, s));
     KC_CUDA(cudaLaunchCooperativeKernel((const void *)hindex_kernel, dim3(grid), dim3(HX_THREADS), args, 0, s));
@@ -390,6 +382,55 @@ int hindex_run(Graph *g, cudaStream_t s, kc_stats *st) {
         st->ms = ms;
     }
     return KC_OK;
+}
+
+static int ensure_events(Graph *g) {
+    if (!g->ev0) {
+        KC_CUDA(cudaEventCreate(&g->ev0));
+        KC_CUDA(cudaEventCreate(&g->ev1));
+        KC_CUDA(cudaEventCreate(&g->evk0));
+        KC_CUDA(cudaEventCreate(&g->evk1));
+    }
+    return KC_OK;
+}
+
+int hindex_run(Graph *g, cudaStream_t s, kc_stats *st) {
+    KC_TRY(ensure_hx_buffers(g));
+    KC_TRY(ensure_events(g));
+    KC_CUDA(cudaEventRecord(g->ev0, s));
+    KC_CUDA(cudaMemsetAsync(g->hctl, 0, sizeof(HindexCtl), s));
+    const int ig = std::max(1, std::min<int>(g->sm_count * 8, (int)((g->n + 255) / 256)));
+    hindex_init<<<ig, 256, 0, s>>>(g->rowptr, g->n, g->core, g->bitmap, g->big[0], g->hctl);
+    return hindex_launch(g, s, st, true);
+}
+
+// Queue the vertices of `list` for sweep 0 (long rows to big[0]); the bitmap
+// must be clear.
+__global__ void hindex_seed(const int64_t *__restrict__ rowptr, const uint32_t *__restrict__ list, uint64_t len,
+                            uint32_t *inlist, uint32_t *small0, uint32_t *big0, HindexCtl *ctl) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < len; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t v = list[i];
+        const unsigned bit = 1u << (v & 31);
+        if (atomicOr(&inlist[v >> 5], bit) & bit) continue;  // listed twice
+        if (rowptr[v + 1] - rowptr[v] > (int64_t)HX_WARP_MAX) big0[atomicAdd(&ctl->big_len[0], 1ull)] = v;
+        else small0[atomicAdd(&ctl->list_len[0], 1ull)] = v;
+    }
+}
+
+// h-index iteration from the current contents of g->core (which must be
+// upper bounds of the core numbers), starting with the vertices of d_list
+// active.  Used by the maintenance of dynamic graphs.
+int hindex_run_from(Graph *g, const uint32_t *d_list, uint64_t len, cudaStream_t s, kc_stats *st) {
+    KC_TRY(ensure_hx_buffers(g));
+    KC_TRY(ensure_events(g));
+    KC_CUDA(cudaEventRecord(g->ev0, s));
+    KC_CUDA(cudaMemsetAsync(g->hctl, 0, sizeof(HindexCtl), s));
+    KC_CUDA(cudaMemsetAsync(g->bitmap, 0, ((uint64_t)g->n + 31) / 32 * 4, s));
+    if (len) {
+        const int ig = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)g->sm_count * 8, (len + 255) / 256));
+        hindex_seed<<<ig, 256, 0, s>>>(g->rowptr, d_list, len, g->bitmap, g->list[0], g->big[0], g->hctl);
+    }
+    return hindex_launch(g, s, st, false);
 }
 
 }  // namespace kc

@@ -7,6 +7,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <string>
+#include <vector>
 
 #include "../../include/kcore.h"
 
@@ -79,6 +80,7 @@ struct Tuning {
     int peel_queues = 1;
     int peel_ctas_per_sm = 0;
     int trace = 0;
+    int64_t update_incremental_max = 65536;  // larger update batches: full recompute
 };
 
 // Control block of the h-index iteration.
@@ -116,6 +118,7 @@ struct Graph {
     unsigned long long *gq = nullptr; // spill queues of work items (sentinel = ~0)
     unsigned long long gq_cap = 0;    // capacity of each of the 3 x gq_nq queues
     unsigned gq_nq = 0;
+    unsigned long long gq_items = 0;  // queue sizing basis (n + nnz / MIN_CHUNK)
     PeelTrace *trace = nullptr;       // per-level trace (when enabled)
     uint32_t trace_cap = 0, trace_count = 0;
     Tuning tune;
@@ -125,6 +128,13 @@ struct Graph {
     uint32_t *big[2] = {nullptr, nullptr};   // h-index high-degree lists
     HindexCtl *hctl = nullptr;
     uint32_t *red = nullptr;          // small reduction scratch (min/max)
+    // dynamic-graph maintenance
+    uint32_t *mfront[2] = {nullptr, nullptr};
+    uint32_t *mcand = nullptr;
+    uint32_t *mvisit = nullptr;
+    unsigned long long *mcount = nullptr;
+    bool simple_checked = false;
+    std::vector<uint32_t> color_count;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, evk0 = nullptr, evk1 = nullptr;
     double last_ms = 0.0, last_kernel_ms = 0.0;
 
@@ -144,6 +154,11 @@ int virtual_layout(Graph *g, uint32_t part_size, uint32_t *h_node_pointer, uint3
 int peel_run(Graph *g, cudaStream_t s, bool gpp_zero_to_one, kc_stats *st);
 // hindex.cu
 int hindex_run(Graph *g, cudaStream_t s, kc_stats *st);
+int hindex_run_from(Graph *g, const uint32_t *d_list, uint64_t len, cudaStream_t s, kc_stats *st);
+
+// maintain.cu
+int graph_update(Graph *g, const uint32_t *ins_src, const uint32_t *ins_dst, uint64_t n_ins, const uint32_t *del_src,
+                 const uint32_t *del_dst, uint64_t n_del, kc_update_stats *st);
 
 // mtx_loader.cpp
 int parse_mtx(const char *path, int mode, uint32_t *n, uint64_t *m, uint32_t **src, uint32_t **dst);

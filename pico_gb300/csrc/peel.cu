@@ -638,7 +638,8 @@ static int ensure_peel_buffers(Graph *g) {
     if (!g->bitmap) KC_TRY(dalloc(&g->bitmap, (n + 31) / 32 + 1, "claim bitmap"));
     if (!g->alive) KC_TRY(dalloc(&g->alive, 2 * n + 2, "alive lists"));
     const unsigned nq = (unsigned)g->tune.peel_queues;
-    if (!g->gq || g->gq_nq != nq) {
+    const unsigned long long items = n + g->nnz / MIN_CHUNK + 64;
+    if (!g->gq || g->gq_nq != nq || g->gq_items < items) {
         // Pushes per level <= n (each vertex is claimed once) + nnz/MIN_CHUNK
         // (row chunks).  Every CTA rotates over the queues one push (<= 32
         // items) at a time, so a queue receives at most total/nq + 32 items
@@ -646,9 +647,10 @@ static int ensure_peel_buffers(Graph *g) {
         // when the slot is recycled; consumed entries are reset to SENT.
         dfree(g->gq);
         g->gq = nullptr;
-        const unsigned long long total = n + g->nnz / MIN_CHUNK + 64;
+        const unsigned long long total = items + items / 4;  // room for the graph to grow
         const unsigned long long ctas = (unsigned long long)g->sm_count * 4;
         g->gq_cap = total / nq + 32 * ctas + 8192;
+        g->gq_items = total;
         KC_TRY(dalloc(&g->gq, 3 * g->gq_cap * nq, "spill queues"));
         g->gq_nq = nq;
         g->gq_clean = false;
