@@ -253,6 +253,62 @@ int kc_batch_free(kc_batch *b);
  * rows of those vertices must reference only [lo, hi). */
 int kc_graph_from_segment(const kc_graph *g, uint32_t lo, uint32_t hi, kc_graph **out);
 
+/* ---- serving: continuous batching of requests on one GPU --------------- */
+/* No counterpart in the reference.  A server keeps `resident` on the device
+ * and runs two request kinds concurrently on separate CUDA streams:
+ * updates (edge batches on the resident graph, exact core maintenance, in
+ * submission order) and decompositions (a graph sent with the request).
+ * Waiting decompositions are admitted as lanes free up and device memory
+ * allows (cudaMemGetInfo minus hbm_reserve_bytes minus what admitted requests
+ * may still allocate); a lane packs all admissible waiting requests (up to
+ * max_batch_graphs / max_batch_bytes) into one batched launch.  Inputs are
+ * copied at submission.  Latency = submission to result on the host. */
+typedef struct kc_server kc_server;
+typedef struct kc_server_config {
+    uint32_t decompose_slots;   /* concurrent decomposition lanes (default 2) */
+    uint32_t max_batch_graphs;  /* requests packed per launch (default 64) */
+    uint64_t max_batch_bytes;   /* estimated device bytes per launch (default 256 MiB) */
+    uint64_t hbm_reserve_bytes; /* device memory left free (0 = none) */
+} kc_server_config;
+typedef struct kc_request_result {
+    int32_t status;             /* KC_OK or the request's error */
+    uint32_t kind;              /* 0 update, 1 decompose */
+    uint32_t n;                 /* vertices of the result */
+    uint32_t kmax;              /* largest core number */
+    uint64_t digest;            /* sum of core[v] * splitmix64(v + 1) mod 2^64 */
+    double latency_ms;          /* submission -> result on host */
+    double queue_ms;            /* submission -> start of work */
+    kc_update_stats update;     /* update requests */
+    uint32_t has_core;          /* a core array is available for kc_server_wait */
+    uint32_t reserved;
+} kc_request_result;
+typedef struct kc_server_stats {
+    uint64_t completed_updates, completed_decompositions, failed;
+    double p50_update_ms, p99_update_ms, p50_decompose_ms, p99_decompose_ms;
+    double elapsed_ms;          /* first submission -> last completion */
+    uint64_t edges_decomposed;  /* undirected edges of completed decompositions */
+    uint64_t edges_updated;     /* edges in completed update batches */
+    uint64_t decompose_launches;
+    uint32_t max_inflight;      /* most requests groups running at once */
+    uint32_t reserved;
+} kc_server_stats;
+/* cfg may be NULL for defaults.  Decomposes `resident` first if needed. */
+int kc_server_create(kc_graph *resident, const kc_server_config *cfg, kc_server **out);
+/* want_core: keep a copy of the full resident core array for kc_server_wait. */
+int kc_server_submit_update(kc_server *s, const uint32_t *ins_src, const uint32_t *ins_dst, uint64_t n_ins,
+                            const uint32_t *del_src, const uint32_t *del_dst, uint64_t n_del, int want_core,
+                            uint64_t *ticket);
+/* A symmetric CSR without self-loops (host memory). */
+int kc_server_submit_decompose(kc_server *s, const int64_t *rowptr, const uint32_t *col, uint32_t n,
+                               uint64_t *ticket);
+/* Blocks until the request is done; fills res, and core_out (capacity
+ * core_cap entries) when a core array is available.  Returns the request's
+ * status.  Each ticket can be waited for once. */
+int kc_server_wait(kc_server *s, uint64_t ticket, kc_request_result *res, uint32_t *core_out, uint64_t core_cap);
+int kc_server_get_stats(kc_server *s, kc_server_stats *st);
+/* Finishes every submitted request, then stops the lanes. */
+int kc_server_free(kc_server *s);
+
 /* ---- memory helpers ----------------------------------------------------
  * The reference allocates and copies inside each driver
  * (peel/src/gpu_memory_allocation.cu:4-21, HistoCore.cu:259-286); callers of

@@ -58,6 +58,27 @@ class kc_update_stats(ctypes.Structure):
                 ("reserved", ctypes.c_uint32), ("ms", ctypes.c_double)]
 
 
+class kc_server_config(ctypes.Structure):
+    _fields_ = [("decompose_slots", ctypes.c_uint32), ("max_batch_graphs", ctypes.c_uint32),
+                ("max_batch_bytes", ctypes.c_uint64), ("hbm_reserve_bytes", ctypes.c_uint64)]
+
+
+class kc_request_result(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int32), ("kind", ctypes.c_uint32), ("n", ctypes.c_uint32),
+                ("kmax", ctypes.c_uint32), ("digest", ctypes.c_uint64), ("latency_ms", ctypes.c_double),
+                ("queue_ms", ctypes.c_double), ("update", kc_update_stats), ("has_core", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32)]
+
+
+class kc_server_stats(ctypes.Structure):
+    _fields_ = [("completed_updates", ctypes.c_uint64), ("completed_decompositions", ctypes.c_uint64),
+                ("failed", ctypes.c_uint64), ("p50_update_ms", ctypes.c_double), ("p99_update_ms", ctypes.c_double),
+                ("p50_decompose_ms", ctypes.c_double), ("p99_decompose_ms", ctypes.c_double),
+                ("elapsed_ms", ctypes.c_double), ("edges_decomposed", ctypes.c_uint64),
+                ("edges_updated", ctypes.c_uint64), ("decompose_launches", ctypes.c_uint64),
+                ("max_inflight", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
 class kc_level_trace(ctypes.Structure):
     _fields_ = [("t_start_ns", ctypes.c_uint64), ("level", ctypes.c_uint32), ("claimed", ctypes.c_uint32),
                 ("scan_len", ctypes.c_uint32), ("spilled", ctypes.c_uint32), ("steals", ctypes.c_uint32),
@@ -143,6 +164,12 @@ def lib():
     _sig(L, "kc_batch_trace", i, [_P, _P, u32])
     _sig(L, "kc_graph_from_segment", i, [_P, u32, u32, PP])
     _sig(L, "kc_graph_update", i, [_P, _P, _P, u64, _P, _P, u64, _P, i, ctypes.POINTER(kc_update_stats)])
+    _sig(L, "kc_server_create", i, [_P, ctypes.POINTER(kc_server_config), PP])
+    _sig(L, "kc_server_submit_update", i, [_P, _P, _P, u64, _P, _P, u64, i, _U64P])
+    _sig(L, "kc_server_submit_decompose", i, [_P, _P, _P, u32, _U64P])
+    _sig(L, "kc_server_wait", i, [_P, u64, ctypes.POINTER(kc_request_result), _P, u64])
+    _sig(L, "kc_server_get_stats", i, [_P, ctypes.POINTER(kc_server_stats)])
+    _sig(L, "kc_server_free", i, [_P])
     _lib = L
     return L
 
@@ -227,9 +254,29 @@ class Graph:
     def __init__(self, handle, device=0):
         self._h = ctypes.c_void_p(handle)
         self.device = device
+
+    def info(self):
+        """(n, nnz, max degree, 32-wide virtual nodes), read from the library
+        (they change when the graph is updated)."""
         n, nnz, md, vn = ctypes.c_uint32(), ctypes.c_uint64(), ctypes.c_uint32(), ctypes.c_uint64()
         check(lib().kc_graph_info(self._h, ctypes.byref(n), ctypes.byref(nnz), ctypes.byref(md), ctypes.byref(vn)))
-        self.n, self.nnz, self.max_degree, self.num_vnodes = n.value, nnz.value, md.value, vn.value
+        return n.value, nnz.value, md.value, vn.value
+
+    @property
+    def n(self):
+        return self.info()[0]
+
+    @property
+    def nnz(self):
+        return self.info()[1]
+
+    @property
+    def max_degree(self):
+        return self.info()[2]
+
+    @property
+    def num_vnodes(self):
+        return self.info()[3]
 
     # ---- construction ----
     @classmethod
@@ -296,10 +343,11 @@ class Graph:
 
     # ---- queries ----
     def csr(self):
-        rowptr = np.empty(self.n + 1, dtype=np.int64)
-        col = np.empty(max(self.nnz, 1), dtype=np.uint32)
+        n, nnz, _, _ = self.info()
+        rowptr = np.empty(n + 1, dtype=np.int64)
+        col = np.empty(max(nnz, 1), dtype=np.uint32)
         check(lib().kc_graph_copy_csr(self._h, _ptr(rowptr), _ptr(col)))
-        return rowptr, col[:self.nnz]
+        return rowptr, col[:nnz]
 
     def degrees(self):
         d = np.empty(max(self.n, 1), dtype=np.uint32)
@@ -372,9 +420,6 @@ class Graph:
         st = kc_update_stats()
         check(lib().kc_graph_update(self._h, _ptr(is_), _ptr(id_), is_.size, _ptr(ds_), _ptr(dd_), ds_.size,
                                     _ptr(core) if want_core else None, 0, ctypes.byref(st)))
-        n, nnz, md, vn = ctypes.c_uint32(), ctypes.c_uint64(), ctypes.c_uint32(), ctypes.c_uint64()
-        check(lib().kc_graph_info(self._h, ctypes.byref(n), ctypes.byref(nnz), ctypes.byref(md), ctypes.byref(vn)))
-        self.nnz, self.max_degree, self.num_vnodes = nnz.value, md.value, vn.value
         stats = {k: getattr(st, k) for k, _ in kc_update_stats._fields_ if k != "reserved"}
         return (core[:self.n] if want_core else None), stats
 
@@ -535,5 +580,71 @@ class Batch:
     def __del__(self):
         try:
             self.free()
+        except Exception:
+            pass
+
+
+def _struct_dict(st):
+    out = {}
+    for k, _ in st._fields_:
+        if k == "reserved":
+            continue
+        v = getattr(st, k)
+        out[k] = _struct_dict(v) if isinstance(v, ctypes.Structure) else v
+    return out
+
+
+class Server:
+    """Continuous-batching request server around a resident graph."""
+
+    def __init__(self, resident, decompose_slots=2, max_batch_graphs=64, max_batch_bytes=256 << 20,
+                 hbm_reserve_bytes=1 << 30):
+        self.resident = resident
+        cfg = kc_server_config(decompose_slots, max_batch_graphs, max_batch_bytes, hbm_reserve_bytes)
+        h = ctypes.c_void_p()
+        check(lib().kc_server_create(resident.handle, ctypes.byref(cfg), ctypes.byref(h)))
+        self._h = h
+        self._keep = {}
+
+    def submit_update(self, ins=None, dels=None, want_core=False):
+        e = np.zeros(0, dtype=np.uint32)
+        is_, id_ = (np.ascontiguousarray(x, dtype=np.uint32) for x in (ins if ins is not None else (e, e)))
+        ds_, dd_ = (np.ascontiguousarray(x, dtype=np.uint32) for x in (dels if dels is not None else (e, e)))
+        t = ctypes.c_uint64()
+        check(lib().kc_server_submit_update(self._h, _ptr(is_), _ptr(id_), is_.size, _ptr(ds_), _ptr(dd_), ds_.size,
+                                            1 if want_core else 0, ctypes.byref(t)))
+        return t.value
+
+    def submit_decompose(self, rowptr, col):
+        rowptr = np.ascontiguousarray(rowptr, dtype=np.int64)
+        col = np.ascontiguousarray(col, dtype=np.uint32)
+        t = ctypes.c_uint64()
+        check(lib().kc_server_submit_decompose(self._h, _ptr(rowptr), _ptr(col), rowptr.size - 1, ctypes.byref(t)))
+        return t.value
+
+    def wait(self, ticket, core_cap=0):
+        res = kc_request_result()
+        core = np.empty(max(core_cap, 1), dtype=np.uint32) if core_cap else None
+        rc = lib().kc_server_wait(self._h, ticket, ctypes.byref(res), _ptr(core) if core_cap else None, core_cap)
+        d = _struct_dict(res)
+        if core is not None and res.has_core:
+            d["core"] = core[:res.n]
+        if rc != KC_OK:
+            raise KCoreError(rc, lib().kc_last_error().decode(errors="replace"))
+        return d
+
+    def stats(self):
+        st = kc_server_stats()
+        check(lib().kc_server_get_stats(self._h, ctypes.byref(st)))
+        return _struct_dict(st)
+
+    def close(self):
+        if self._h is not None and self._h.value:
+            check(lib().kc_server_free(self._h))
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
         except Exception:
             pass

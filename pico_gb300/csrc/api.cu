@@ -24,25 +24,34 @@ int fail(int code, const char *fmt, ...) {
 
 void clear_error() { g_last_error.clear(); }
 
+// Device memory comes from the stream-ordered pool allocator: unlike
+// cudaMalloc / cudaFree it does not synchronize the whole device, so work of
+// independent graphs (server lanes) keeps overlapping.  Allocation is ordered
+// on the legacy stream and waited for, so the memory is usable from any
+// stream; every caller has finished its own stream's work on a buffer before
+// freeing it.
 int dmalloc(void **p, size_t bytes, const char *what) {
     *p = nullptr;
-    cudaError_t e = cudaMalloc(p, bytes);
+    cudaError_t e = cudaMallocAsync(p, bytes, cudaStreamLegacy);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(cudaStreamLegacy);
     if (e != cudaSuccess) {
         cudaGetLastError();
+        if (*p) cudaFreeAsync(*p, cudaStreamLegacy);
         *p = nullptr;
-        return fail(KC_ERR_NOMEM, "cudaMalloc(%zu bytes) for %s: %s", bytes, what, cudaGetErrorString(e));
+        return fail(KC_ERR_NOMEM, "device allocation of %zu bytes for %s: %s", bytes, what, cudaGetErrorString(e));
     }
     return KC_OK;
 }
 
 void dfree(void *p) {
-    if (p) cudaFree(p);
+    if (p) cudaFreeAsync(p, cudaStreamLegacy);
 }
 
 Graph::~Graph() {
     int cur = 0;
     cudaGetDevice(&cur);
     cudaSetDevice(device);
+    if (stream) cudaStreamSynchronize(stream);
     dfree(rowptr);
     dfree(col);
     dfree(core);
