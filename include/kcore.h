@@ -316,10 +316,11 @@ int kc_server_free(kc_server *s);
 /* Pinned host memory (fast host<->device copies). */
 int kc_host_alloc(void **p, size_t bytes);
 int kc_host_free(void *p);
-/* Device memory on `device`. */
+/* Device memory on `device` (stream-ordered pool).  Free a buffer only after
+ * the work that uses it has completed. */
 int kc_device_alloc(void **p, size_t bytes, int device);
 int kc_device_free(void *p);
-/* cudaMemcpy; kind: 1 = host->device, 2 = device->host, 3 = device->device. */
+/* Blocking copy; kind: 1 = host->device, 2 = device->host, 3 = device->device. */
 int kc_memcpy(void *dst, const void *src, size_t bytes, int kind);
 /* Wait for all work on `device` to finish. */
 int kc_device_synchronize(int device);

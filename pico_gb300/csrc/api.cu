@@ -523,7 +523,12 @@ int kc_device_alloc(void **p, size_t bytes, int device) {
 
 int kc_device_free(void *p) {
     clear_error();
-    if (p) KC_CUDA(cudaFree(p));
+    // ordered after earlier work on the legacy stream (e.g. a device-to-device
+    // kc_memcpy), like every free of pool memory in this library
+    if (p) {
+        KC_CUDA(cudaFreeAsync(p, cudaStreamLegacy));
+        KC_CUDA(cudaStreamSynchronize(cudaStreamLegacy));
+    }
     return KC_OK;
 }
 
@@ -535,6 +540,8 @@ int kc_memcpy(void *dst, const void *src, size_t bytes, int kind) {
                                  : (kind == 2 ? cudaMemcpyDeviceToHost : (kind == 3 ? cudaMemcpyDeviceToDevice : cudaMemcpyDefault));
     if (kind < 1 || kind > 3) return fail(KC_ERR_INVALID, "copy kind %d", kind);
     KC_CUDA(cudaMemcpy(dst, src, bytes, k));
+    // a device-to-device cudaMemcpy may return before the copy is done
+    if (kind == 3) KC_CUDA(cudaStreamSynchronize(cudaStreamLegacy));
     return KC_OK;
 }
 
