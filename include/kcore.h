@@ -309,6 +309,22 @@ int kc_server_get_stats(kc_server *s, kc_server_stats *st);
 /* Finishes every submitted request, then stops the lanes. */
 int kc_server_free(kc_server *s);
 
+/* ---- allocation-free decomposition -------------------------------------- */
+/* No counterpart in the reference.  Core numbers of one small graph for
+ * callers that cannot allocate device memory on this path (a framework that
+ * owns all device memory through its own pool, a latency-critical loop where
+ * cudaMalloc/cudaFree would synchronize the device).  Inputs and output are
+ * device pointers on the current device: rowptr[n+1] (int64), col[rowptr[n]]
+ * (symmetric, no self-loops), core[n].  Limits: n <= 50,000 vertices and
+ * rowptr[n] <= 4,194,304 entries; larger graphs get KC_ERR_CAPACITY.  The
+ * only scratch is a fixed array of about 663 KB inside the library that every
+ * GPU loading it holds until exit; it is looked up on the first call on each
+ * device (make that first call before any stream capture).  All calls share
+ * it: calls that overlap on the GPU race and must be serialised by the caller.
+ * Nothing is allocated.  Blocks until the result is in core. */
+int kc_decompose_noalloc(const int64_t *d_rowptr, const uint32_t *d_col, uint32_t n, uint32_t *d_core,
+                         void *stream);
+
 /* ---- memory helpers ----------------------------------------------------
  * The reference allocates and copies inside each driver
  * (peel/src/gpu_memory_allocation.cu:4-21, HistoCore.cu:259-286); callers of

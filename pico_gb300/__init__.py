@@ -170,6 +170,7 @@ def lib():
     _sig(L, "kc_server_wait", i, [_P, u64, ctypes.POINTER(kc_request_result), _P, u64])
     _sig(L, "kc_server_get_stats", i, [_P, ctypes.POINTER(kc_server_stats)])
     _sig(L, "kc_server_free", i, [_P])
+    _sig(L, "kc_decompose_noalloc", i, [_P, _P, u32, _P, _P])
     _lib = L
     return L
 

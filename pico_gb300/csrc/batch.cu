@@ -25,6 +25,7 @@
 // configurations on the batch itself and keeps the fastest.
 #include <algorithm>
 #include <cstring>
+#include <mutex>
 #include <numeric>
 #include <string>
 #include <vector>
@@ -716,3 +717,112 @@ int kc_batch_free(kc_batch *b) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free decomposition of one small graph.
+//
+// For callers that cannot allocate device memory on this path: code running
+// under a framework that owns all device memory through its own pool (so a
+// cudaMalloc by this library would break its budget), latency-critical loops
+// where cudaMalloc/cudaFree would synchronize the device, and code paths that
+// must not create allocations at all.  The caller passes the graph and the
+// output in device memory; the only scratch the batched kernel needs -- its
+// row-chunk queue and a few control words -- lives in the fixed file-scope
+// array below, which every GPU that loads this library holds until the
+// process exits.  All calls share that array: calls whose work overlaps on
+// the GPU (different streams, or different host threads) race on it and must
+// be serialised by the caller.
+namespace kc {
+
+constexpr uint32_t NOALLOC_MAX_N = 50000;            // vertices
+constexpr uint64_t NOALLOC_MAX_NNZ = 1ull << 22;     // directed CSR entries
+constexpr uint64_t NOALLOC_CTRL_WORDS = 32;          // control block (256 bytes)
+constexpr uint64_t NOALLOC_QUEUE = NOALLOC_MAX_N + NOALLOC_MAX_NNZ / BATCH_MIN_CHUNK + 2;
+constexpr uint64_t NOALLOC_WORDS = NOALLOC_CTRL_WORDS + NOALLOC_QUEUE;  // 8-byte words, ~663 KB
+
+static __device__ __align__(256) unsigned long long g_noalloc_scratch[NOALLOC_WORDS];
+
+// Writes the one-graph work list into the control block: vbase = {0, n},
+// order = {0}, fbase = {0}, work counter = 0.
+__global__ void noalloc_prep(unsigned long long *scratch, uint32_t n) {
+    uint32_t *w = reinterpret_cast<uint32_t *>(scratch);
+    w[0] = 0;  // vbase[0]
+    w[1] = n;  // vbase[1]
+    w[2] = 0;  // order[0]
+    w[4] = 0;  // next (work counter)
+    scratch[3] = 0ull;  // fbase[0]
+}
+
+static std::mutex g_noalloc_mu;
+static void *g_noalloc_ptr[64];
+
+// Device address of the scratch array, looked up once per device with that
+// device current (a host-side use of the symbol's name is not a device
+// address).
+static int noalloc_setup(int dev, unsigned long long **out) {
+    if (dev < 0 || dev >= 64) return fail(KC_ERR_INVALID, "device %d out of range", dev);
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p)
+            return fail(KC_ERR_CUDA, "cudaGetSymbolAddress(no-alloc scratch): %s", cudaGetErrorString(e));
+        const size_t smem = ((NOALLOC_MAX_N * sizeof(uint32_t) + 15) & ~size_t(15)) + ((NOALLOC_MAX_N + 31) / 32) * 4 + 16;
+        e = cudaFuncSetAttribute(batch_peel<uint32_t, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return fail(KC_ERR_CUDA, "no-alloc kernel setup: %s", cudaGetErrorString(e));
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = static_cast<unsigned long long *>(g_noalloc_ptr[dev]);
+    return KC_OK;
+}
+
+}  // namespace kc
+
+extern "C" int kc_decompose_noalloc(const int64_t *d_rowptr, const uint32_t *d_col, uint32_t n, uint32_t *d_core,
+                                    void *stream) {
+    using namespace kc;
+    clear_error();
+    if (!d_rowptr || !d_core || (n && !d_col)) return fail(KC_ERR_INVALID, "null argument");
+    if (n > NOALLOC_MAX_N)
+        return fail(KC_ERR_CAPACITY, "kc_decompose_noalloc: %u vertices exceed the limit of %u", n, NOALLOC_MAX_N);
+    int dev = 0;
+    KC_CUDA(cudaGetDevice(&dev));
+    unsigned long long *scratch = nullptr;
+    KC_TRY(noalloc_setup(dev, &scratch));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    int64_t nnz = 0;
+    KC_CUDA(cudaMemcpyAsync(&nnz, d_rowptr + n, sizeof(nnz), cudaMemcpyDeviceToHost, s));
+    KC_CUDA(cudaStreamSynchronize(s));
+    if (nnz < 0 || (uint64_t)nnz > NOALLOC_MAX_NNZ)
+        return fail(KC_ERR_CAPACITY, "kc_decompose_noalloc: %lld entries exceed the limit of %llu", (long long)nnz,
+                    (unsigned long long)NOALLOC_MAX_NNZ);
+    if (n == 0) return KC_OK;
+    noalloc_prep<<<1, 1, 0, s>>>(scratch, n);
+    uint32_t *ctrl = reinterpret_cast<uint32_t *>(scratch);
+    BatchArgs A;
+    A.rowptr = d_rowptr;
+    A.col = d_col;
+    A.core = d_core;
+    A.vbase = ctrl;
+    A.order = ctrl + 2;
+    A.count = 1;
+    A.F = scratch + NOALLOC_CTRL_WORDS;
+    A.fbase = scratch + 3;
+    A.next = ctrl + 4;
+    A.gdeg = nullptr;
+    A.gclaimed = nullptr;
+    A.chunk = 256;
+    A.smem_n = (n + 31) & ~31u;
+    A.gtrace = nullptr;
+    const size_t smem = ((A.smem_n * sizeof(uint32_t) + 15) & ~size_t(15)) + ((A.smem_n + 31) / 32) * 4 + 16;
+    {
+        // the batch planner sets this kernel's shared-memory limit for its own
+        // launches; restore what this launch needs right before it
+        std::lock_guard<std::mutex> lk(g_noalloc_mu);
+        KC_CUDA(cudaFuncSetAttribute(batch_peel<uint32_t, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        batch_peel<uint32_t, true><<<1, 1024, smem, s>>>(A);
+    }
+    KC_CUDA(cudaGetLastError());
+    KC_CUDA(cudaStreamSynchronize(s));
+    return KC_OK;
+}
