@@ -346,9 +346,125 @@ def run_engine(args, wl, world, rank, local, dist):
     for p in (h_rp, h_col, h_core):
         pg.lib().kc_host_free(p)
     g.free()
+    if world == 1 and not args.no_batch:
+        line["batched"] = batch_section(pg, device, sptr, args.steps, args.warmup, args.batch_graphs)
+    if world == 1 and not args.no_serve:
+        line["serving"] = serve_section(pg, device, args.serve_requests, args.serve_rate)
     if rank == 0:
         print(json.dumps(line), flush=True)
     return 0
+
+
+BATCH_DESC = ("4096 graphs, n = floor(10^U(2,5)), generator uniform over Erdos-Renyi / R-MAT (a,b,c=.57,.19,.19) / "
+              "Barabasi-Albert (m_BA in 1..32), average degree U[4,64], seed 4, packed as one segmented CSR")
+
+
+def batch_section(pg, device, sptr, steps, warmup, num_graphs=4096):
+    """Batched (one launch, CUDA graph, autotuned) against the plain form (one
+    decomposition call per graph) over the same 4096 graphs; both results are
+    compared graph by graph."""
+    import numpy as np
+    import torch
+
+    from pico_gb300 import workloads
+    t_gen = time.perf_counter()
+    g, vbase, _ = workloads.batch_mix(num_graphs, seed=4, device=device)
+    gen_s = time.perf_counter() - t_gen
+    n, nnz = g.n, g.nnz
+    m = nnz // 2
+    b = pg.Batch(g, vbase)
+    tuned_ms = b.autotune()
+    for _ in range(warmup):
+        b.decompose_device(stream=sptr)
+    torch.cuda.synchronize(device)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    stream = torch.cuda.ExternalStream(sptr, device=device)
+    ev0.record(stream)
+    for _ in range(steps):
+        b.decompose_device(stream=sptr)
+    ev1.record(stream)
+    torch.cuda.synchronize(device)
+    batched_ms = ev0.elapsed_time(ev1) / steps
+    core_b, _ = b.decompose(stream=sptr)
+
+    G = vbase.size - 1
+    segs = [g.segment(int(vbase[i]), int(vbase[i + 1])) for i in range(G)]
+    for h in segs:
+        h.decompose_device("peelone_dyn", stream=sptr)
+    torch.cuda.synchronize(device)
+    t0 = time.perf_counter()
+    for h in segs:
+        h.decompose_device("peelone_dyn", stream=sptr)
+    torch.cuda.synchronize(device)
+    plain_ms = 1e3 * (time.perf_counter() - t0)
+    same = True
+    for i, h in enumerate(segs):
+        c, _ = h.decompose("peelone_dyn", stream=sptr)
+        if not np.array_equal(c, core_b[int(vbase[i]):int(vbase[i + 1])]):
+            same = False
+        h.free()
+    kb, kp = b.get_param("batch.small_n"), b.get_param("batch.small_threads")
+    kc = b.get_param("batch.chunk")
+    b.free()
+    g.free()
+    return {
+        "workload": BATCH_DESC.replace("4096", str(G), 1), "graphs": G, "n_total": n, "m_undirected_total": m, "nnz_total": nnz,
+        "value": round(m / (batched_ms / 1e3) / 1e6, 3), "unit": "M edges/s", "ms_per_step": round(batched_ms, 4),
+        "steps": steps, "plain_value": round(m / (plain_ms / 1e3) / 1e6, 3), "plain_ms": round(plain_ms, 2),
+        "plain_form": "one kc_decompose(KC_PEELONE_DYN) call per graph over the same device-resident graphs",
+        "batched_over_plain": round(plain_ms / batched_ms, 2), "identical_results": same,
+        "autotuned": {"batch.small_n": kb, "batch.small_threads": kp, "batch.chunk": kc,
+                      "best_ms": round(tuned_ms, 4)},
+        "generate_s": round(gen_s, 2),
+    }
+
+
+def serve_section(pg, device, requests, rate_hz):
+    """A Poisson stream of edge-update batches (against a resident R-MAT
+    scale-22 graph) and decompositions of fresh batch-mix-style graphs,
+    submitted at their arrival times to the continuous-batching server."""
+    import numpy as np
+
+    from pico_gb300 import workloads
+    base = pg.rmat_graph(22, 16, 2, device=device)
+    rp, col = base.csr()
+    t_gen = time.perf_counter()
+    reqs = workloads.serve_stream(rp, col, requests, seed=5, rate_hz=rate_hz, device=device)
+    gen_s = time.perf_counter() - t_gen
+    del rp, col
+    srv = pg.Server(base, decompose_slots=2, max_batch_graphs=64)
+    t0 = time.perf_counter()
+    res = workloads.run_stream(srv, reqs, realtime=True)
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    base.free()
+    lat = np.array([r["latency_ms"] for r in res])
+    upd = [r for q, r in zip(reqs, res) if q["kind"] == "update"]
+    dec = [r for q, r in zip(reqs, res) if q["kind"] == "decompose"]
+    upd_edges = sum(q["ins"][0].size + q["dels"][0].size for q in reqs if q["kind"] == "update")
+    dec_edges = sum(int(q["rowptr"][-1]) // 2 for q in reqs if q["kind"] == "decompose")
+
+    def pct(x, p):
+        return round(float(np.percentile(x, p)), 3) if len(x) else None
+
+    return {
+        "workload": ("resident R-MAT scale 22 ef 16 (seed 2); Poisson arrivals at %g req/s, seed 5; half edge-update "
+                     "batches of floor(10^U(3,6)) edges (50/50 insert/delete), half decompositions of a fresh "
+                     "batch-mix-style graph" % rate_hz),
+        "requests": len(reqs), "updates": len(upd), "decompositions": len(dec),
+        "p50_ms": pct(lat, 50), "p99_ms": pct(lat, 99),
+        "p50_update_ms": pct([r["latency_ms"] for r in upd], 50),
+        "p99_update_ms": pct([r["latency_ms"] for r in upd], 99),
+        "p50_decompose_ms": pct([r["latency_ms"] for r in dec], 50),
+        "p99_decompose_ms": pct([r["latency_ms"] for r in dec], 99),
+        "throughput_req_s": round(len(reqs) / wall, 2),
+        "throughput_m_edges_s": round((upd_edges + dec_edges) / wall / 1e6, 3),
+        "failed": int(st["failed"]), "decompose_launches": int(st["decompose_launches"]),
+        "max_inflight": int(st["max_inflight"]), "latency": "submission (arrival) to result on host",
+        "generate_s": round(gen_s, 2),
+    }
 
 
 def main():
@@ -362,6 +478,11 @@ def main():
     ap.add_argument("--clock-window", type=float, default=1.5,
                     help="seconds of identical load before the timed steps, so clocks are sampled under load")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 4096-graph batched-vs-plain section")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving section")
+    ap.add_argument("--batch-graphs", type=int, default=4096, help="graphs in the batched section")
+    ap.add_argument("--serve-requests", type=int, default=40)
+    ap.add_argument("--serve-rate", type=float, default=20.0, help="Poisson arrival rate, requests/s")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

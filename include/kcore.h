@@ -178,7 +178,11 @@ int kc_graph_last_timing(const kc_graph *g, double *total_ms, double *kernel_ms)
  * of shared queues, 1..64), "peel.ctas_per_sm" (0 = occupancy maximum),
  * "trace" (1 = record a per-level trace of the next decompositions),
  * "update.incremental_max" (largest update batch, in edges, maintained
- * incrementally by kc_graph_update). */
+ * incrementally by kc_graph_update), "wait.timeout_us" (limit of one
+ * inter-CTA wait of the peel and h-index kernels, default 2 s; a wait that
+ * runs out makes the call return KC_ERR_TIMEOUT), "test.withhold" (1 = one
+ * CTA never signals the others, so their waits run out: exercises the
+ * timeout path without faulting the GPU; off by default). */
 int kc_graph_set_param(kc_graph *g, const char *name, int64_t value);
 
 /* Per-level trace of the last peel decomposition (recorded when the "trace"

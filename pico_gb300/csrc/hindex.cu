@@ -47,6 +47,7 @@ struct HxArgs {
     unsigned long long timeout_ns;
     uint32_t max_sweeps;
     uint32_t first_all;  // sweep 0 covers every vertex (else list[0] / big[0])
+    uint32_t withhold;   // CTA 0 never arrives at the first barrier (failure-detection hook)
 };
 
 __global__ void hindex_init(const int64_t *__restrict__ rowptr, uint32_t n, uint32_t *c, uint32_t *inlist,
@@ -263,6 +264,21 @@ __global__ void __launch_bounds__(HX_THREADS, 2) hindex_kernel(HxArgs A) {
     const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     HindexCtl *ctl = A.ctl;
     const unsigned G = gridDim.x;
+    if (A.withhold && blockIdx.x == 0) {
+        // The barrier count never reaches the grid size: the other CTAs' waits
+        // run into their limit.  This CTA waits (bounded) for their verdict.
+        if (threadIdx.x == 0) {
+            const unsigned long long t0 = global_ns();
+            while (ld_relaxed(&ctl->err) == 0u) {
+                if (global_ns() - t0 > A.timeout_ns) {
+                    atomicCAS(&ctl->err, 0u, (unsigned)KC_ERR_TIMEOUT);
+                    break;
+                }
+                __nanosleep(1000);
+            }
+        }
+        return;
+    }
     for (uint32_t sweep = 0;; sweep++) {
         const unsigned cur = sweep & 1, nxt = cur ^ 1;
         if (threadIdx.x == 0) changed_sh = 0;
@@ -355,7 +371,8 @@ static int hindex_launch(Graph *g, cudaStream_t s, kc_stats *st, bool first_all)
     A.big[0] = g->big[0];
     A.big[1] = g->big[1];
     A.ctl = g->hctl;
-    A.timeout_ns = 20ull * 1000 * 1000 * 1000;
+    A.timeout_ns = (unsigned long long)g->tune.wait_timeout_us * 1000ull;
+    A.withhold = (unsigned)g->tune.withhold;
     A.max_sweeps = g->n + 3;  // a path needs O(n) sweeps
     A.first_all = first_all ? 1u : 0u;
     void *args[] = {&A};

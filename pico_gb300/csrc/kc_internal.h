@@ -81,6 +81,8 @@ struct Tuning {
     int peel_ctas_per_sm = 0;
     int trace = 0;
     int64_t update_incremental_max = 65536;  // larger update batches: full recompute
+    int64_t wait_timeout_us = 2000000;       // limit of one inter-CTA wait
+    int withhold = 0;  // failure-detection hook: one CTA never signals, so the others' waits run out
 };
 
 // Control block of the h-index iteration.

@@ -67,6 +67,7 @@ struct PeelArgs {
     unsigned spill_t;            // cascade items a CTA keeps locally
     unsigned steal_max;          // items per steal
     unsigned nq;                 // shared queues in use
+    unsigned withhold;           // CTA 0 keeps one credit of level index 1 (failure-detection hook)
 };
 
 // Initialisation and level 0 in one streaming pass: residual degrees from the
@@ -163,6 +164,7 @@ __global__ void __launch_bounds__(PEEL_THREADS, 2) peel_kernel(PeelArgs A) {
     __shared__ unsigned long long wait_t0;
     __shared__ unsigned int warp_cnt[SCAN_U][PEEL_WARPS];
     __shared__ unsigned long long next_tile;
+    __shared__ unsigned int withheld;
 
     const unsigned tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const unsigned G = gridDim.x;
@@ -179,6 +181,7 @@ __global__ void __launch_bounds__(PEEL_THREADS, 2) peel_kernel(PeelArgs A) {
         spill_rr = blockIdx.x;
         res_mask = 0;
         steal_cnt = 0;
+        withheld = 0;
     }
     __syncthreads();
     if (level_sh == NO_LEVEL) {  // every vertex had degree 0
@@ -272,7 +275,14 @@ __global__ void __launch_bounds__(PEEL_THREADS, 2) peel_kernel(PeelArgs A) {
                             atomicMax(&ctl->kmax, L);
                         }
                         __threadfence();
-                        atomicAdd(&ctl->pending[s], (unsigned long long)(0ull - credit));
+                        unsigned long long give = credit;
+                        if (A.withhold && blockIdx.x == 0 && li == 1 && !withheld) {
+                            // the level's count can no longer reach zero: every
+                            // CTA's wait runs into its limit
+                            give -= 1;
+                            withheld = 1;
+                        }
+                        atomicAdd(&ctl->pending[s], (unsigned long long)(0ull - give));
                         credit = 0;
                     }
                     // Shared queues: a CTA reserves up to steal_max slots with one
@@ -706,7 +716,8 @@ int peel_run(Graph *g, cudaStream_t s, bool gpp_zero_to_one_flag, kc_stats *st) 
     A.ctl = g->peel_ctl;
     A.trace = g->tune.trace ? g->trace : nullptr;
     A.trace_cap = g->tune.trace ? g->trace_cap : 0;
-    A.timeout_ns = 20ull * 1000 * 1000 * 1000;
+    A.timeout_ns = (unsigned long long)g->tune.wait_timeout_us * 1000ull;
+    A.withhold = (unsigned)g->tune.withhold;
     A.max_level_indices = g->max_deg + 3;
     A.chunk = (unsigned)g->tune.peel_chunk;
     A.spill_t = (unsigned)g->tune.peel_spill;
