@@ -298,7 +298,10 @@ def run_engine(args, wl, world, rank, local, dist):
                      "frac": round(achieved / peak, 4), "traffic": traffic, "peak_kind": peak_kind,
                      "kernel": kernel_name, "bytes_per_launch": bytes_alg,
                      "kernel_ms_avg": round(kavg, 4)},
-        "gpu_launches": args.steps * (2 if kernel_name == "peel_kernel" else 3),
+        # kernels per decomposition: peel_ctl_reset + peel_init + peel_kernel
+        # (+ gpp_zero_to_one for gppeel); hindex_init + hindex_kernel
+        "gpu_launches": args.steps * ((4 if pg.method_id(method) == 4 else 3) if kernel_name == "peel_kernel"
+                                      else 2),
         "clocks": sampler.summary(t_load0, t_load1),
     }
 

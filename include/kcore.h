@@ -195,6 +195,9 @@ typedef struct kc_level_trace {
     uint32_t spilled;     /* items published on the shared queues */
     uint32_t steals;      /* successful steals */
     uint32_t steal_fail;  /* failed steal attempts */
+    uint64_t t_work_end_ns; /* GPU global timer when the last CTA handed back its work credit */
+    uint32_t rounds;      /* most processing rounds of one CTA */
+    uint32_t max_steal;   /* largest single steal (items) */
 } kc_level_trace;
 int kc_graph_trace(const kc_graph *g, kc_level_trace *out, uint32_t cap, uint32_t *count);
 

@@ -71,6 +71,8 @@ struct PeelCtl {
 struct PeelTrace {
     unsigned long long t_start_ns;
     unsigned int level, claimed, scan_len, spilled, steals, steal_fail;
+    unsigned long long t_work_end_ns;
+    unsigned int rounds, max_steal;
 };
 
 struct Tuning {
