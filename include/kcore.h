@@ -132,6 +132,24 @@ int kc_graph_from_csr(const int64_t *rowptr, const uint32_t *col, uint32_t n, in
 int kc_graph_from_csr_device(const int64_t *d_rowptr, const uint32_t *d_col, uint32_t n, int device,
                              kc_graph **out);
 
+/* Binary edge list: a file of little-endian uint32 (src, dst) pairs, 0-based
+ * ids, n = largest id + 1, read through mmap (no text parsing); flags as for
+ * kc_graph_from_edges.  The fast input path for graphs whose MatrixMarket
+ * text takes minutes to parse (the reference parses text only,
+ * index2core/shared/graph.cpp:17-95, peel/src/graph.cpp:58-133). */
+int kc_graph_from_edge_file(const char *path, uint32_t flags, int device, kc_graph **out);
+
+/* Binary snapshot of a graph and, when a decomposition has completed, its core
+ * numbers: a 64-byte header (magic "KCSNAP01", version, flags, n, nnz, a 64-bit
+ * content hash of the payload) followed by rowptr int64[n+1], col uint32[nnz]
+ * (padded to 8 bytes) and core uint32[n].  kc_graph_load rejects a file whose
+ * size or content hash does not match its header, and restores the core
+ * numbers (kc_graph_device_core works without a new decomposition).  Replaces
+ * the reference's text CSR cache (peel/src/graph.cpp:9-54,151), which is keyed
+ * by the input's basename only. */
+int kc_graph_save(const kc_graph *g, const char *path);
+int kc_graph_load(const char *path, int device, kc_graph **out);
+
 /* Check symmetry / self-loops / id range on the device.  *bad = number of
  * offending entries (0 for a valid graph). */
 int kc_graph_validate(kc_graph *g, uint64_t *bad);
@@ -176,6 +194,10 @@ int kc_graph_last_timing(const kc_graph *g, double *total_ms, double *kernel_ms)
  * item), "peel.spill" (cascade items a CTA keeps before publishing to the
  * shared queues), "peel.steal" (most items reserved per steal, 1..64), "peel.queues" (number
  * of shared queues, 1..64), "peel.ctas_per_sm" (0 = occupancy maximum),
+ * "peel.unroll" (row entries each lane keeps in flight, 4 or 8),
+ * "peel.threads" (threads per CTA, 512 or 256), "peel.balanced" (1 = each
+ * processing round spreads at most "peel.round_entries" row entries evenly
+ * over the CTA's threads),
  * "trace" (1 = record a per-level trace of the next decompositions),
  * "update.incremental_max" (largest update batch, in edges, maintained
  * incrementally by kc_graph_update), "wait.timeout_us" (limit of one
@@ -203,6 +225,15 @@ int kc_graph_trace(const kc_graph *g, kc_level_trace *out, uint32_t cap, uint32_
 
 /* Device pointer of the last decomposition's core array (n uint32). */
 int kc_graph_device_core(const kc_graph *g, const uint32_t **d_core);
+
+/* The induced k-core of the last decomposition as a graph of its own: the
+ * vertices with core >= k, renumbered in increasing id order, and the edges
+ * among them (rows keep their order).  map_out (optional; host memory, or
+ * device memory when map_on_device is 1) receives the original id of each new
+ * vertex and needs room for every vertex with core >= k.  The reference prints
+ * only the largest and smallest core (util.cpp:6-22); this extends its result
+ * writers (utility::SaveResults, util.cpp:70-89). */
+int kc_graph_kcore_subgraph(const kc_graph *g, uint32_t k, kc_graph **out, uint32_t *map_out, int map_on_device);
 
 /* ---- dynamic graphs: exact core maintenance under edge batches ---------- */
 /* No counterpart in the reference (its "dyn" drivers use dynamic work

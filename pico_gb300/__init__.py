@@ -164,6 +164,10 @@ def lib():
     _sig(L, "kc_batch_free", i, [_P])
     _sig(L, "kc_batch_trace", i, [_P, _P, u32])
     _sig(L, "kc_graph_from_segment", i, [_P, u32, u32, PP])
+    _sig(L, "kc_graph_save", i, [_P, ctypes.c_char_p])
+    _sig(L, "kc_graph_load", i, [ctypes.c_char_p, i, PP])
+    _sig(L, "kc_graph_from_edge_file", i, [ctypes.c_char_p, u32, i, PP])
+    _sig(L, "kc_graph_kcore_subgraph", i, [_P, u32, PP, _P, i])
     _sig(L, "kc_graph_update", i, [_P, _P, _P, u64, _P, _P, u64, _P, i, ctypes.POINTER(kc_update_stats)])
     _sig(L, "kc_server_create", i, [_P, ctypes.POINTER(kc_server_config), PP])
     _sig(L, "kc_server_submit_update", i, [_P, _P, _P, u64, _P, _P, u64, i, _U64P])
@@ -424,6 +428,42 @@ class Graph:
                                     _ptr(core) if want_core else None, 0, ctypes.byref(st)))
         stats = {k: getattr(st, k) for k, _ in kc_update_stats._fields_ if k != "reserved"}
         return (core[:self.n] if want_core else None), stats
+
+    def save(self, path):
+        """Binary snapshot (CSR, and the core numbers when a decomposition has completed)."""
+        check(lib().kc_graph_save(self._h, os.fsencode(path)))
+
+    @classmethod
+    def load(cls, path, device=0):
+        """Graph from a snapshot written by save(); its core numbers come back too."""
+        h = ctypes.c_void_p()
+        check(lib().kc_graph_load(os.fsencode(path), device, ctypes.byref(h)))
+        return cls(h.value, device)
+
+    @classmethod
+    def from_edge_file(cls, path, dedup=False, sort_rows=False, device=0):
+        """Graph from a binary file of little-endian uint32 (src, dst) pairs."""
+        flags = (EDGES_DEDUP if dedup else 0) | (EDGES_SORT_ROWS if sort_rows else 0)
+        h = ctypes.c_void_p()
+        check(lib().kc_graph_from_edge_file(os.fsencode(path), flags, device, ctypes.byref(h)))
+        return cls(h.value, device)
+
+    def kcore_subgraph(self, k):
+        """(Graph of the induced k-core, original ids uint32[n']) of the last decomposition."""
+        core = self.core()
+        cnt = int((core >= k).sum())
+        ids = np.zeros(max(cnt, 1), dtype=np.uint32)
+        h = ctypes.c_void_p()
+        check(lib().kc_graph_kcore_subgraph(self._h, int(k), ctypes.byref(h), _ptr(ids), 0))
+        return Graph(h.value, self.device), ids[:cnt]
+
+    def core(self):
+        """Core numbers of the last decomposition (host copy of the device result)."""
+        p = self.device_core()
+        out = np.empty(max(self.n, 1), dtype=np.uint32)
+        if self.n:
+            check(lib().kc_memcpy(_ptr(out), ctypes.c_void_p(p), 4 * self.n, 2))
+        return out[:self.n]
 
     def segment(self, lo, hi):
         """Standalone graph of vertices [lo, hi) (ids rebased to 0)."""

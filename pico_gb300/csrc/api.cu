@@ -106,6 +106,8 @@ static int new_graph(int device, kc_graph **out) {
     return KC_OK;
 }
 
+int graph_new(int device, kc_graph **out) { return new_graph(device, out); }
+
 __global__ void core_minmax(const uint32_t *__restrict__ c, uint32_t n, uint32_t *mm) {
     uint32_t mn = 0xffffffffu, mx = 0;
     for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n; v += (uint64_t)gridDim.x * blockDim.x) {
@@ -436,6 +438,17 @@ int kc_graph_set_param(kc_graph *g, const char *name, int64_t value) {
     } else if (k == "peel.ctas_per_sm") {
         if (value < 0 || value > 32) return fail(KC_ERR_INVALID, "peel.ctas_per_sm: [0, 32]");
         t.peel_ctas_per_sm = (int)value;
+    } else if (k == "peel.unroll") {
+        if (value != 4 && value != 8) return fail(KC_ERR_INVALID, "peel.unroll: 4 or 8");
+        t.peel_unroll = (int)value;
+    } else if (k == "peel.threads") {
+        if (value != 256 && value != 512) return fail(KC_ERR_INVALID, "peel.threads: 256 or 512");
+        t.peel_threads = (int)value;
+    } else if (k == "peel.balanced") {
+        t.peel_balanced = value ? 1 : 0;
+    } else if (k == "peel.round_entries") {
+        if (value < 256 || value > (1 << 24)) return fail(KC_ERR_INVALID, "peel.round_entries: [256, 2^24]");
+        t.peel_round_entries = (int)value;
     } else if (k == "trace") {
         t.trace = value ? 1 : 0;
     } else if (k == "update.incremental_max") {

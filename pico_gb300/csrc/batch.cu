@@ -641,7 +641,10 @@ int kc_batch_decompose(kc_batch *b, uint32_t *core_out, int out_on_device, kc_st
     KC_CUDA(cudaSetDevice(g->device));
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : g->stream;
     KC_CUDA(cudaEventRecord(b->ev0, s));
-    KC_TRY(run_batch(b, s));
+    if (int rc = run_batch(b, s)) {
+        cudaStreamSynchronize(s);  // nothing launched may outlive a failed call
+        return rc;
+    }
     KC_CUDA(cudaEventRecord(b->ev1, s));
     if (core_out && g->n)
         KC_CUDA(cudaMemcpyAsync(core_out, g->core, (uint64_t)g->n * 4,

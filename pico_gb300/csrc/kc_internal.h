@@ -81,6 +81,10 @@ struct Tuning {
     int peel_steal = 64;
     int peel_queues = 1;
     int peel_ctas_per_sm = 0;
+    int peel_unroll = 4;  // row entries in flight per lane: 4 or 8
+    int peel_threads = 512;  // threads per CTA: 512 (2 per SM) or 256 (4 per SM)
+    int peel_balanced = 0;   // 1: rounds spread a bounded number of row entries over the whole CTA
+    int peel_round_entries = 4096;
     int trace = 0;
     int64_t update_incremental_max = 65536;  // larger update batches: full recompute
     int64_t wait_timeout_us = 2000000;       // limit of one inter-CTA wait
@@ -181,3 +185,8 @@ int edges_offset(uint32_t *d_src, uint32_t *d_dst, uint64_t m, uint32_t off, cud
 }  // namespace kc
 
 struct kc_graph : kc::Graph {};
+
+namespace kc {
+// An empty graph handle on `device` with its own stream (api.cu).
+int graph_new(int device, kc_graph **out);
+}  // namespace kc

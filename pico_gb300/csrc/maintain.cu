@@ -228,7 +228,11 @@ __global__ void endpoints(const uint32_t *__restrict__ src, const uint32_t *__re
 }
 
 // Temporary device arrays freed on scope exit.
+// Scratch arrays of one call, freed when the call returns (after the call's
+// stream has finished with them, so an early error return cannot free memory
+// that a launched kernel still uses).
 struct Scratch {
+    cudaStream_t stream = nullptr;
     std::vector<void *> ptrs;
     template <class T>
     int get(T **p, uint64_t count, const char *what) {
@@ -237,6 +241,7 @@ struct Scratch {
         return rc;
     }
     ~Scratch() {
+        if (stream && !ptrs.empty()) cudaStreamSynchronize(stream);
         for (void *p : ptrs) dfree(p);
     }
 };
@@ -266,6 +271,7 @@ static int apply_changes(Graph *g, const uint32_t *d_isrc, const uint32_t *d_ids
         if (rc) return rc;
     }
     Scratch sc;
+    sc.stream = s;
     uint32_t *dpos = nullptr, *dcnt = nullptr, *ival = nullptr, *icnt = nullptr, *newlen = nullptr;
     unsigned long long *applied = nullptr;
     if (md) {
@@ -388,6 +394,7 @@ int graph_update(Graph *g, const uint32_t *ins_src, const uint32_t *ins_dst, uin
     }
     if (!g->core_valid) KC_TRY(peel_run(g, s, false, nullptr));
     Scratch sc;
+    sc.stream = s;
     const bool incremental = n_ins + n_del <= (uint64_t)g->tune.update_incremental_max;
     uint32_t *d_del_s = nullptr, *d_del_d = nullptr;
     if (n_del) {

@@ -36,14 +36,10 @@
 
 namespace kc {
 
-constexpr int PEEL_THREADS = 512;
-constexpr int PEEL_WARPS = PEEL_THREADS / 32;
 constexpr unsigned QCAP = 4096;       // shared-memory queue capacity (items)
 constexpr unsigned LOW_WATER = 1024;  // take a new scan tile only below this queue size
 constexpr int SCAN_U = 4;             // alive-list entries per thread per scan tile
-constexpr unsigned TILE = PEEL_THREADS * SCAN_U;
 constexpr unsigned MIN_CHUNK = 256;   // smallest row chunk (sizes the shared queues)
-constexpr int PEEL_U = 4;             // row entries in flight per lane
 constexpr unsigned long long SENT = ~0ull;
 constexpr unsigned int NO_LEVEL = 0xffffffffu;
 
@@ -67,6 +63,7 @@ struct PeelArgs {
     unsigned spill_t;            // cascade items a CTA keeps locally
     unsigned steal_max;          // items per steal
     unsigned nq;                 // shared queues in use
+    unsigned round_e;            // balanced rounds: row entries a CTA takes per round
     unsigned withhold;           // CTA 0 keeps one credit of level index 1 (failure-detection hook)
 };
 
@@ -149,7 +146,13 @@ __device__ __forceinline__ void set_err(PeelCtl *ctl, unsigned code, unsigned in
     if (atomicCAS(&ctl->err, 0u, code) == 0u) ctl->err_info = info;
 }
 
-__global__ void __launch_bounds__(PEEL_THREADS, 2) peel_kernel(PeelArgs A) {
+// PEEL_U: row entries each lane keeps in flight while walking rows; NT:
+// threads per CTA (two CTAs of 512 or four of 256 per SM, 64 registers each).
+template <int PEEL_U, int NT, bool BAL>
+__global__ void __launch_bounds__(NT, 1024 / NT) peel_kernel(PeelArgs A) {
+    constexpr int PEEL_THREADS = NT;
+    constexpr int PEEL_WARPS = NT / 32;
+    constexpr unsigned TILE = NT * SCAN_U;
     __shared__ unsigned long long q[QCAP];
     __shared__ unsigned int q_head, q_tail;
     __shared__ int mode;
@@ -165,6 +168,11 @@ __global__ void __launch_bounds__(PEEL_THREADS, 2) peel_kernel(PeelArgs A) {
     __shared__ unsigned int warp_cnt[SCAN_U][PEEL_WARPS];
     __shared__ unsigned long long next_tile;
     __shared__ unsigned int withheld;
+    __shared__ unsigned int rounds_sh;
+    __shared__ unsigned int bal_off[BAL ? NT + 1 : 1];  // balanced rounds: item offsets,
+    __shared__ int64_t bal_rs[BAL ? NT : 1];            // row starts,
+    __shared__ unsigned int bal_wsum[NT / 32];          // per-warp sums
+    __shared__ unsigned int bal_take;                   // and item count
 
     const unsigned tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const unsigned G = gridDim.x;
@@ -233,6 +241,7 @@ __global__ void __launch_bounds__(PEEL_THREADS, 2) peel_kernel(PeelArgs A) {
             min_sh = NO_LEVEL;
             claimed_any = 0;
             wait_t0 = 0;
+            rounds_sh = 0;
         }
         __syncthreads();
 
@@ -252,22 +261,31 @@ __global__ void __launch_bounds__(PEEL_THREADS, 2) peel_kernel(PeelArgs A) {
                     }
                 }
                 if (!md && qsize > 0) {
-                    unsigned per = (qsize + PEEL_WARPS - 1) / PEEL_WARPS;
-                    if (per > 32) per = 32;
-                    unsigned take = min(qsize, per * PEEL_WARPS);
-                    b_base = q_head;
-                    b_per_warp = per;
-                    b_take = take;
-                    q_head += take;
+                    if constexpr (BAL) {
+                        // candidates; the round itself decides how many it takes
+                        b_base = q_head;
+                        b_take = min(qsize, (unsigned)NT);
+                    } else {
+                        unsigned per = (qsize + PEEL_WARPS - 1) / PEEL_WARPS;
+                        if (per > 32) per = 32;
+                        unsigned take = min(qsize, per * PEEL_WARPS);
+                        b_base = q_head;
+                        b_per_warp = per;
+                        b_take = take;
+                        q_head += take;
+                    }
                     md = M_PROC;
+                    rounds_sh++;
                 }
                 if (!md) {
                     // idle: hand back the credits held, after publishing this
                     // CTA's level minimum and claim flag
                     if (credit > 0) {
-                        if (A.trace && li < A.trace_cap && claims_sh) {
-                            atomicAdd(&A.trace[li].claimed, claims_sh);
+                        if (A.trace && li < A.trace_cap) {
+                            if (claims_sh) atomicAdd(&A.trace[li].claimed, claims_sh);
                             claims_sh = 0;
+                            atomicMax(&A.trace[li].rounds, rounds_sh);
+                            atomicMax(&A.trace[li].t_work_end_ns, global_ns());
                         }
                         if (min_sh != NO_LEVEL) atomicMin(&ctl->next_min[s], min_sh);
                         if (claimed_any) {
@@ -305,7 +323,10 @@ __global__ void __launch_bounds__(PEEL_THREADS, 2) peel_kernel(PeelArgs A) {
                                 if (r + want > A.gq_cap) want = A.gq_cap - r;
                                 res_base = ((unsigned long long)s * A.nq + qi) * A.gq_cap + r;
                                 res_mask = want >= 64 ? ~0ull : ((1ull << want) - 1);
-                                if (A.trace && li < A.trace_cap) atomicAdd(&A.trace[li].steals, 1u);
+                                if (A.trace && li < A.trace_cap) {
+                                    atomicAdd(&A.trace[li].steals, 1u);
+                                    atomicMax(&A.trace[li].max_steal, (unsigned)want);
+                                }
                             }
                             probe = qi;
                             break;
@@ -456,13 +477,25 @@ __global__ void __launch_bounds__(PEEL_THREADS, 2) peel_kernel(PeelArgs A) {
                 continue;
             }
 
-            // ---- M_PROC: each warp expands its share of the queue ----------
+            // ---- M_PROC ------------------------------------------------------
+            // Unbalanced form: each warp expands the concatenated rows of its
+            // own share of the queued items.  Balanced form (BAL): the CTA
+            // takes queued items up to a budget of A.round_e row entries and
+            // spreads those entries evenly over all its threads, so a round
+            // never outlasts a few dependent memory round trips and a claim
+            // made in it is picked up in the next round.
             {
-                const unsigned my_lo = b_base + warp * b_per_warp;
-                const unsigned my_hi = min(my_lo + b_per_warp, b_base + b_take);
-                const unsigned nit = my_hi > my_lo ? my_hi - my_lo : 0u;
                 unsigned long long item = SENT;
-                if (lane < nit) item = q[(my_lo + lane) % QCAP];
+                unsigned nit;
+                if constexpr (BAL) {
+                    nit = tid < b_take ? 1u : 0u;
+                    if (nit) item = q[(b_base + tid) % QCAP];
+                } else {
+                    const unsigned my_lo = b_base + warp * b_per_warp;
+                    const unsigned my_hi = min(my_lo + b_per_warp, b_base + b_take);
+                    nit = my_hi > my_lo ? my_hi - my_lo : 0u;
+                    if (lane < nit) item = q[(my_lo + lane) % QCAP];
+                }
                 int64_t rs = 0;
                 uint32_t len = 0;
                 bool hub = false;
@@ -474,6 +507,37 @@ __global__ void __launch_bounds__(PEEL_THREADS, 2) peel_kernel(PeelArgs A) {
                     int64_t re = min(r1, rs + (int64_t)A.chunk);
                     len = re > rs ? (uint32_t)(re - rs) : 0u;
                     hub = (c == 0 && r1 - r0 > (int64_t)A.chunk);
+                }
+                unsigned total;
+                unsigned off = warp_excl_scan(len, lane, total);
+                if constexpr (BAL) {
+                    // CTA-wide exclusive scan of the item lengths
+                    if (lane == 0) bal_wsum[warp] = total;
+                    __syncthreads();
+                    unsigned wbase = 0, ctot = 0;
+#pragma unroll
+                    for (int w2 = 0; w2 < PEEL_WARPS; w2++) {
+                        const unsigned x = bal_wsum[w2];
+                        wbase += (w2 < (int)warp) ? x : 0u;
+                        ctot += x;
+                    }
+                    off += wbase;
+                    // the items that start within the budget (a prefix)
+                    const bool inb = nit && off < A.round_e;
+                    const unsigned take = (unsigned)__syncthreads_count(inb);
+                    if (inb) {
+                        bal_off[tid] = off;
+                        bal_rs[tid] = rs;
+                    }
+                    if (tid + 1 == take) bal_off[take] = off + len;
+                    if (tid == 0) {
+                        q_head = b_base + take;  // the rest stays queued
+                        bal_take = take;
+                    }
+                    hub = hub && inb;
+                    (void)ctot;
+                    __syncthreads();
+                    total = bal_off[bal_take];
                 }
                 // split hub rows: chunk items 1..k-1 go to the global queue
                 unsigned hubs = __ballot_sync(KC_FULL_MASK, hub);
@@ -505,24 +569,37 @@ __global__ void __launch_bounds__(PEEL_THREADS, 2) peel_kernel(PeelArgs A) {
                                          ((unsigned long long)v << 32) | (c0 + lane + 1));
                     }
                 }
-                // expand the concatenated rows of this warp's items; each lane
-                // keeps PEEL_U entries in flight (loads, then bitmap probes,
-                // then decrements) so the round trips overlap
-                unsigned total;
-                unsigned off = warp_excl_scan(len, lane, total);
-                const bool single = __ballot_sync(KC_FULL_MASK, len != 0) == 1u;  // one item, in lane 0
+                // expand the rows; each thread keeps PEEL_U entries in flight
+                // (loads, then bitmap probes, then decrements) so the round
+                // trips overlap
+                constexpr unsigned SPAN = BAL ? (unsigned)NT : 32u;  // threads sharing the rows
+                const unsigned me = BAL ? tid : lane;
+                const bool single = !BAL && __ballot_sync(KC_FULL_MASK, len != 0) == 1u;  // one item, in lane 0
                 unsigned local_min = NO_LEVEL;
                 unsigned wclaims = 0;
-                for (unsigned base = 0; base < total; base += 32 * PEEL_U) {
+                for (unsigned base = 0; base < total; base += SPAN * PEEL_U) {
                     uint32_t u[PEEL_U];
                     unsigned a[PEEL_U];
                     bool live[PEEL_U];
 #pragma unroll
                     for (int k = 0; k < PEEL_U; k++) {
-                        const unsigned e = base + k * 32 + lane;
+                        const unsigned e = base + k * SPAN + me;
                         int64_t rj;
                         unsigned oj;
-                        if (single) {
+                        live[k] = e < total;
+                        if constexpr (BAL) {
+                            // owner item: the last j with bal_off[j] <= e
+                            unsigned lo = 0, hi2 = bal_take;
+                            if (live[k]) {
+                                while (hi2 - lo > 1) {
+                                    const unsigned mid = (lo + hi2) >> 1;
+                                    if (bal_off[mid] <= e) lo = mid;
+                                    else hi2 = mid;
+                                }
+                            }
+                            rj = bal_rs[lo];
+                            oj = bal_off[lo];
+                        } else if (single) {
                             rj = __shfl_sync(KC_FULL_MASK, rs, 0);
                             oj = 0;
                         } else {
@@ -537,7 +614,6 @@ __global__ void __launch_bounds__(PEEL_THREADS, 2) peel_kernel(PeelArgs A) {
                             rj = __shfl_sync(KC_FULL_MASK, rs, j);
                             oj = __shfl_sync(KC_FULL_MASK, off, j);
                         }
-                        live[k] = e < total;
                         u[k] = live[k] ? __ldcs(&A.col[rj + (e - oj)]) : 0u;
                     }
 #pragma unroll
@@ -675,9 +751,21 @@ static int ensure_peel_buffers(Graph *g) {
     return KC_OK;
 }
 
-static int peel_grid(int sm_count, int ctas_per_sm, int *grid) {
+// The kernel variant selected by the tunables, and its thread count.
+static const void *peel_variant(const Tuning &t, int *threads) {
+    *threads = t.peel_threads;
+    const bool b = t.peel_balanced != 0, u8 = t.peel_unroll == 8;
+    if (t.peel_threads == 256) {
+        if (b) return u8 ? (const void *)peel_kernel<8, 256, true> : (const void *)peel_kernel<4, 256, true>;
+        return u8 ? (const void *)peel_kernel<8, 256, false> : (const void *)peel_kernel<4, 256, false>;
+    }
+    if (b) return u8 ? (const void *)peel_kernel<8, 512, true> : (const void *)peel_kernel<4, 512, true>;
+    return u8 ? (const void *)peel_kernel<8, 512, false> : (const void *)peel_kernel<4, 512, false>;
+}
+
+static int peel_grid(const void *kern, int threads, int sm_count, int ctas_per_sm, int *grid) {
     int occ = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, peel_kernel, PEEL_THREADS, 0);
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, threads, 0);
     if (e != cudaSuccess) return fail(KC_ERR_CUDA, "occupancy query: %s", cudaGetErrorString(e));
     if (occ < 1) return fail(KC_ERR_UNSUPPORTED, "peel kernel cannot be resident");
     if (ctas_per_sm > 0 && ctas_per_sm < occ) occ = ctas_per_sm;
@@ -693,7 +781,9 @@ int peel_run(Graph *g, cudaStream_t s, bool gpp_zero_to_one_flag, kc_stats *st) 
     cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, g->device);
     if (!coop) return fail(KC_ERR_UNSUPPORTED, "device lacks cooperative launch");
     int grid = 0;
-    KC_TRY(peel_grid(g->sm_count, g->tune.peel_ctas_per_sm, &grid));
+    int threads = 0;
+    const void *kern = peel_variant(g->tune, &threads);
+    KC_TRY(peel_grid(kern, threads, g->sm_count, g->tune.peel_ctas_per_sm, &grid));
     if (!g->gq_clean) {
         KC_CUDA(cudaMemsetAsync(g->gq, 0xff, 3 * g->gq_cap * g->gq_nq * sizeof(unsigned long long), s));
         g->gq_clean = true;
@@ -723,6 +813,7 @@ int peel_run(Graph *g, cudaStream_t s, bool gpp_zero_to_one_flag, kc_stats *st) 
     A.spill_t = (unsigned)g->tune.peel_spill;
     A.steal_max = (unsigned)g->tune.peel_steal;
     A.nq = nq_of(g);
+    A.round_e = (unsigned)g->tune.peel_round_entries;
     KC_CUDA(cudaEventRecord(g->ev0, s));
     if (A.trace) KC_CUDA(cudaMemsetAsync(g->trace, 0, sizeof(PeelTrace) * g->trace_cap, s));
     const int ig = std::max(1, std::min<int>(g->sm_count * 8, (int)((g->n + 255) / 256)));
@@ -730,7 +821,7 @@ int peel_run(Graph *g, cudaStream_t s, bool gpp_zero_to_one_flag, kc_stats *st) 
     peel_init<<<ig, 256, 0, s>>>(g->rowptr, g->n, g->core, g->bitmap, g->alive + g->n, g->peel_ctl, (unsigned)grid);
     void *args[] = {&A};
     KC_CUDA(cudaEventRecord(g->evk0, s));
-    KC_CUDA(cudaLaunchCooperativeKernel((const void *)peel_kernel, dim3(grid), dim3(PEEL_THREADS), args, 0, s));
+    KC_CUDA(cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(threads), args, 0, s));
     KC_CUDA(cudaEventRecord(g->evk1, s));
     if (gpp_zero_to_one_flag && g->n)
         gpp_zero_to_one<<<ig, 256, 0, s>>>(g->rowptr, g->n, g->core);

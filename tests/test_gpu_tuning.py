@@ -1,6 +1,6 @@
 """The peel's work-accounting protocol under extreme tunables: everything
 spilled to the shared queues, one item per steal, 1..64 queues, tiny and large
-row chunks, one CTA per SM.  Every setting must give the exact core numbers."""
+row chunks, one CTA per SM, both CTA sizes and both unroll depths.  Every setting must give the exact core numbers."""
 import numpy as np
 import pytest
 
@@ -18,6 +18,14 @@ SETTINGS = [
     {"peel.spill": 3072, "peel.steal": 64, "peel.chunk": 65536},
     {"peel.ctas_per_sm": 1, "peel.queues": 32},
     {"peel.chunk": 256, "peel.steal": 5, "peel.queues": 3},
+    {"peel.unroll": 8},
+    {"peel.threads": 256},
+    {"peel.threads": 256, "peel.unroll": 8, "peel.spill": 0, "peel.steal": 2},
+    {"peel.threads": 256, "peel.ctas_per_sm": 1, "peel.queues": 16},
+    {"peel.balanced": 1},
+    {"peel.balanced": 1, "peel.round_entries": 256, "peel.spill": 0, "peel.steal": 1},
+    {"peel.balanced": 1, "peel.round_entries": 1 << 20, "peel.unroll": 8},
+    {"peel.balanced": 1, "peel.threads": 256, "peel.chunk": 65536, "peel.queues": 5},
 ]
 
 
