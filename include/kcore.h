@@ -197,7 +197,8 @@ int kc_graph_last_timing(const kc_graph *g, double *total_ms, double *kernel_ms)
  * "peel.unroll" (row entries each lane keeps in flight, 4 or 8),
  * "peel.threads" (threads per CTA, 512 or 256), "peel.balanced" (1 = each
  * processing round spreads at most "peel.round_entries" row entries evenly
- * over the CTA's threads),
+ * over the CTA's threads), "peel.scan_unroll" (alive-list entries per
+ * thread per scan tile, 4 or 8),
  * "trace" (1 = record a per-level trace of the next decompositions),
  * "update.incremental_max" (largest update batch, in edges, maintained
  * incrementally by kc_graph_update), "wait.timeout_us" (limit of one
@@ -220,6 +221,7 @@ typedef struct kc_level_trace {
     uint64_t t_work_end_ns; /* GPU global timer when the last CTA handed back its work credit */
     uint32_t rounds;      /* most processing rounds of one CTA */
     uint32_t max_steal;   /* largest single steal (items) */
+    uint64_t cta_ns[4];   /* CTA time summed over CTAs: scanning, processing rows, stealing, idle */
 } kc_level_trace;
 int kc_graph_trace(const kc_graph *g, kc_level_trace *out, uint32_t cap, uint32_t *count);
 

@@ -83,7 +83,7 @@ class kc_level_trace(ctypes.Structure):
     _fields_ = [("t_start_ns", ctypes.c_uint64), ("level", ctypes.c_uint32), ("claimed", ctypes.c_uint32),
                 ("scan_len", ctypes.c_uint32), ("spilled", ctypes.c_uint32), ("steals", ctypes.c_uint32),
                 ("steal_fail", ctypes.c_uint32), ("t_work_end_ns", ctypes.c_uint64), ("rounds", ctypes.c_uint32),
-                ("max_steal", ctypes.c_uint32)]
+                ("max_steal", ctypes.c_uint32), ("cta_ns", ctypes.c_uint64 * 4)]
 
 
 @dataclass

@@ -54,6 +54,8 @@ struct BatchArgs {
     uint32_t chunk;
     uint32_t smem_n;                  // vertex capacity of the shared-memory arrays
     unsigned long long *gtrace;       // per graph: start ns, end ns, SM id (or nullptr)
+    uint32_t *alist;                  // two alive lists per graph (packed ids + packed n), or nullptr
+    uint32_t alist_stride;            // packed vertex count: offset of the second list
 };
 
 // SMEM: degrees + claim bitmap in shared memory; otherwise global memory.
@@ -90,6 +92,7 @@ template <typename DegT, bool SMEM>
 __global__ void batch_peel(BatchArgs A) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ unsigned int gi_sh, fcount, fhead, minnext, end_sh;
+    __shared__ unsigned int list_len, kept_sh, use_list, cur_list, compact_sh;
     const unsigned tid = threadIdx.x, lane = tid & 31, nthreads = blockDim.x;
     for (;;) {
         if (tid == 0) gi_sh = atomicAdd(A.next, 1u);
@@ -126,6 +129,12 @@ __global__ void batch_peel(BatchArgs A) {
             for (uint32_t v = tid; v < n; v += nthreads) flags[v] = 0;
         }
         unsigned L = 0;
+        if (tid == 0) {
+            list_len = n;  // the first levels scan 0..n-1 directly
+            use_list = 0;
+            cur_list = 0;
+            kept_sh = n;
+        }
         __syncthreads();
         // Queues the row of claimed vertex v as chunk-sized items (warp-wide
         // call).  An item holds its row range itself -- start << 24 | length --
@@ -153,14 +162,23 @@ __global__ void batch_peel(BatchArgs A) {
             if (tid == 0) {
                 fcount = 0;
                 minnext = NO_LVL;
+                // rewrite the alive list once fewer than half of its entries
+                // survived the last scan
+                compact_sh = (A.alist != nullptr && kept_sh < list_len / 2) ? 1u : 0u;
+                kept_sh = 0;
             }
             __syncthreads();
             unsigned my_min = NO_LVL;
-            // ---- one scan per level: claim every vertex at or below L ----
-            for (uint32_t b = 0; b < n; b += nthreads) {
-                const uint32_t v = b + tid;
-                bool take = false;
-                if (v < n && !is_claimed<DegT, SMEM>(bits, flags, v)) {
+            const unsigned len = list_len, compact = compact_sh;
+            const uint32_t *lin = use_list ? A.alist + (size_t)cur_list * A.alist_stride + v0 : nullptr;
+            uint32_t *lout = A.alist ? A.alist + (size_t)(cur_list ^ 1u) * A.alist_stride + v0 : nullptr;
+            // ---- one scan per level over the alive list: claim every vertex
+            // at or below L, count (or, when compacting, rewrite) the rest ----
+            for (uint32_t b = 0; b < len; b += nthreads) {
+                const uint32_t i = b + tid;
+                const uint32_t v = i < len ? (lin ? lin[i] : i) : 0xffffffffu;
+                bool take = false, keep = false;
+                if (v != 0xffffffffu && !is_claimed<DegT, SMEM>(bits, flags, v)) {
                     const unsigned d = deg[v];
                     if (d <= L) {
                         take = true;
@@ -168,12 +186,25 @@ __global__ void batch_peel(BatchArgs A) {
                         if (SMEM) atomicOr(&bits[v >> 5], 1u << (v & 31));
                         else flags[v] = 1;
                     } else {
+                        keep = true;
                         my_min = min(my_min, d);
                     }
+                }
+                const unsigned km = __ballot_sync(KC_FULL_MASK, keep);
+                unsigned kb = 0;
+                if (lane == 0 && km) kb = atomicAdd(&kept_sh, (unsigned)__popc(km));
+                if (compact) {
+                    kb = __shfl_sync(KC_FULL_MASK, kb, 0);
+                    if (keep) lout[kb + __popc(km & ((1u << lane) - 1u))] = v;
                 }
                 enqueue(take, v);
             }
             __syncthreads();
+            if (tid == 0 && compact) {
+                list_len = kept_sh;
+                use_list = 1;
+                cur_list ^= 1u;
+            }
             // ---- expansion rounds: cascades land behind the current round ----
             unsigned start = 0;
             for (;;) {
@@ -329,6 +360,7 @@ struct kc_batch {
     unsigned int *d_next = nullptr;  // one counter per class
     uint32_t *d_gdeg = nullptr;
     uint8_t *d_gclaimed = nullptr;
+    uint32_t *d_alist = nullptr;  // two alive lists over the packed vertex ids
     kc::BatchConfig cfg;
     std::vector<kc::BatchClass> classes;
     bool planned = false;
@@ -418,6 +450,7 @@ static int plan(kc_batch *b) {
         }
         b->classes.push_back(std::move(c));
     }
+    if (!b->d_alist) KC_TRY(dalloc(&b->d_alist, 2 * (uint64_t)b->g->n + 2, "batch alive lists"));
     b->planned = true;
     return KC_OK;
 }
@@ -448,6 +481,8 @@ static int launch_all(kc_batch *b, cudaStream_t s) {
         A.chunk = b->cfg.chunk;
         A.smem_n = c.smem_n;
         A.gtrace = b->trace ? b->d_gtrace : nullptr;
+        A.alist = b->d_alist;
+        A.alist_stride = b->g->n;
         if (c.kind <= 1) batch_peel<uint16_t, true><<<c.grid, c.threads, c.smem_bytes, cs>>>(A);
         else if (c.kind == 2) batch_peel<uint32_t, true><<<c.grid, c.threads, c.smem_bytes, cs>>>(A);
         else batch_peel<uint32_t, false><<<c.grid, c.threads, 0, cs>>>(A);
@@ -501,6 +536,7 @@ kc_batch::~kc_batch() {
     kc::dfree(d_next);
     kc::dfree(d_gdeg);
     kc::dfree(d_gclaimed);
+    kc::dfree(d_alist);
     kc::dfree(d_gtrace);
     for (int i = 0; i < 3; i++) {
         if (side[i]) cudaStreamDestroy(side[i]);
@@ -817,6 +853,8 @@ extern "C" int kc_decompose_noalloc(const int64_t *d_rowptr, const uint32_t *d_c
     A.chunk = 256;
     A.smem_n = (n + 31) & ~31u;
     A.gtrace = nullptr;
+    A.alist = nullptr;  // scans the vertex range every level: no list storage
+    A.alist_stride = 0;
     const size_t smem = ((A.smem_n * sizeof(uint32_t) + 15) & ~size_t(15)) + ((A.smem_n + 31) / 32) * 4 + 16;
     {
         // the batch planner sets this kernel's shared-memory limit for its own

@@ -73,18 +73,20 @@ struct PeelTrace {
     unsigned int level, claimed, scan_len, spilled, steals, steal_fail;
     unsigned long long t_work_end_ns;
     unsigned int rounds, max_steal;
+    unsigned long long cta_ns[4];  // CTA time summed over CTAs: scan, process, steal, idle
 };
 
 struct Tuning {
-    int peel_chunk = 256;
+    int peel_chunk = 1024;
     int peel_spill = 32;
     int peel_steal = 64;
     int peel_queues = 1;
     int peel_ctas_per_sm = 0;
     int peel_unroll = 4;  // row entries in flight per lane: 4 or 8
     int peel_threads = 512;  // threads per CTA: 512 (2 per SM) or 256 (4 per SM)
-    int peel_balanced = 0;   // 1: rounds spread a bounded number of row entries over the whole CTA
-    int peel_round_entries = 4096;
+    int peel_balanced = 1;   // 1: rounds spread a bounded number of row entries over the whole CTA
+    int peel_round_entries = 16384;
+    int peel_scan_unroll = 4;  // alive-list entries per thread per scan tile: 4 or 8
     int trace = 0;
     int64_t update_incremental_max = 65536;  // larger update batches: full recompute
     int64_t wait_timeout_us = 2000000;       // limit of one inter-CTA wait

@@ -36,9 +36,7 @@
 
 namespace kc {
 
-constexpr unsigned QCAP = 4096;       // shared-memory queue capacity (items)
 constexpr unsigned LOW_WATER = 1024;  // take a new scan tile only below this queue size
-constexpr int SCAN_U = 4;             // alive-list entries per thread per scan tile
 constexpr unsigned MIN_CHUNK = 256;   // smallest row chunk (sizes the shared queues)
 constexpr unsigned long long SENT = ~0ull;
 constexpr unsigned int NO_LEVEL = 0xffffffffu;
@@ -147,9 +145,14 @@ __device__ __forceinline__ void set_err(PeelCtl *ctl, unsigned code, unsigned in
 }
 
 // PEEL_U: row entries each lane keeps in flight while walking rows; NT:
-// threads per CTA (two CTAs of 512 or four of 256 per SM, 64 registers each).
-template <int PEEL_U, int NT, bool BAL>
+// threads per CTA (two CTAs of 512 or four of 256 per SM, 64 registers each);
+// BAL: balanced processing rounds; SCAN_U: alive-list entries per thread per
+// scan tile.
+template <int PEEL_U, int NT, bool BAL, int SCAN_U>
 __global__ void __launch_bounds__(NT, 1024 / NT) peel_kernel(PeelArgs A) {
+    constexpr unsigned QCAP = 4096u;  // shared-memory queue capacity (items)
+    // a scan tile is taken only while the queue has room for all its claims
+    constexpr unsigned SCAN_BELOW = LOW_WATER < QCAP - NT * SCAN_U + 1 ? LOW_WATER : QCAP - NT * SCAN_U + 1;
     constexpr int PEEL_THREADS = NT;
     constexpr int PEEL_WARPS = NT / 32;
     constexpr unsigned TILE = NT * SCAN_U;
@@ -169,6 +172,8 @@ __global__ void __launch_bounds__(NT, 1024 / NT) peel_kernel(PeelArgs A) {
     __shared__ unsigned long long next_tile;
     __shared__ unsigned int withheld;
     __shared__ unsigned int rounds_sh;
+    __shared__ unsigned long long mode_ns[4], mode_t0;  // trace: time per mode in this level
+    __shared__ int prev_mode;
     __shared__ unsigned int bal_off[BAL ? NT + 1 : 1];  // balanced rounds: item offsets,
     __shared__ int64_t bal_rs[BAL ? NT : 1];            // row starts,
     __shared__ unsigned int bal_wsum[NT / 32];          // per-warp sums
@@ -242,6 +247,11 @@ __global__ void __launch_bounds__(NT, 1024 / NT) peel_kernel(PeelArgs A) {
             claimed_any = 0;
             wait_t0 = 0;
             rounds_sh = 0;
+            if (A.trace) {
+                mode_ns[0] = mode_ns[1] = mode_ns[2] = mode_ns[3] = 0;
+                mode_t0 = global_ns();
+                prev_mode = M_SPIN;
+            }
         }
         __syncthreads();
 
@@ -250,7 +260,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) peel_kernel(PeelArgs A) {
                 int md = 0;
                 unsigned qsize = q_tail - q_head;
                 if (ld_relaxed(&ctl->err) != 0) md = M_EXIT;
-                if (!md && !scan_done && qsize < LOW_WATER) {
+                if (!md && !scan_done && qsize < SCAN_BELOW) {
                     unsigned long long t = next_tile * TILE;
                     if (t < scan_len) {
                         tile_base = t;
@@ -356,6 +366,14 @@ __global__ void __launch_bounds__(NT, 1024 / NT) peel_kernel(PeelArgs A) {
                     }
                 }
                 mode = md;
+                if (A.trace) {
+                    const unsigned long long now = global_ns();
+                    const int pm = prev_mode;
+                    const int slot = pm == M_SCAN ? 0 : pm == M_PROC ? 1 : pm == M_STEAL ? 2 : 3;
+                    mode_ns[slot] += now - mode_t0;
+                    mode_t0 = now;
+                    prev_mode = md;
+                }
             }
             __syncthreads();
             const int md = mode;
@@ -394,7 +412,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) peel_kernel(PeelArgs A) {
             if (md == M_SCAN) {
                 // ---- scan one tile (SCAN_U entries per thread) of the alive list
                 uint32_t v[SCAN_U];
-                unsigned w[SCAN_U], d[SCAN_U];
+                unsigned d[SCAN_U];
                 bool inr[SCAN_U], keep[SCAN_U], take[SCAN_U], push[SCAN_U];
 #pragma unroll
                 for (int k = 0; k < SCAN_U; k++) {
@@ -402,13 +420,15 @@ __global__ void __launch_bounds__(NT, 1024 / NT) peel_kernel(PeelArgs A) {
                     inr[k] = pos < scan_len;
                     v[k] = inr[k] ? src[pos] : 0u;
                 }
+                // The residual degree alone sorts the entries: a vertex peeled
+                // at an earlier level holds its level (< L); one peeled at this
+                // level holds L, or less while a clamped decrement is being
+                // undone; a survivor holds more than L.  So no claim-bit read is
+                // needed: entries at or below L try to claim, and the atomicOr
+                // that claims returns whether someone (a relaxer, or this scan
+                // at an earlier level) already had.
 #pragma unroll
-                for (int k = 0; k < SCAN_U; k++) w[k] = inr[k] ? __ldcg(&A.claimed[v[k] >> 5]) : 0xffffffffu;
-#pragma unroll
-                for (int k = 0; k < SCAN_U; k++) {
-                    inr[k] = inr[k] && !(w[k] & (1u << (v[k] & 31)));
-                    d[k] = inr[k] ? __ldcg(&A.deg[v[k]]) : 0u;
-                }
+                for (int k = 0; k < SCAN_U; k++) d[k] = inr[k] ? __ldcg(&A.deg[v[k]]) : 0u;
                 unsigned dkeep = NO_LEVEL;
 #pragma unroll
                 for (int k = 0; k < SCAN_U; k++) {
@@ -694,6 +714,11 @@ __global__ void __launch_bounds__(NT, 1024 / NT) peel_kernel(PeelArgs A) {
 
         // ---- level boundary (all CTAs saw the level's credits reach zero) ----
         __syncthreads();
+        if (tid == 0 && A.trace && li < A.trace_cap) {
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+                if (mode_ns[i]) atomicAdd(&A.trace[li].cta_ns[i], mode_ns[i]);
+        }
         if (tid == 0) {
             unsigned nxt = NO_LEVEL;
             if (mode == M_DONE) {
@@ -752,15 +777,24 @@ static int ensure_peel_buffers(Graph *g) {
 }
 
 // The kernel variant selected by the tunables, and its thread count.
+template <int U, int NT, bool B>
+static const void *peel_variant_su(int scan_u) {
+    return scan_u == 8 ? (const void *)peel_kernel<U, NT, B, 8> : (const void *)peel_kernel<U, NT, B, 4>;
+}
+
+template <int U, int NT>
+static const void *peel_variant_b(const Tuning &t) {
+    return t.peel_balanced ? peel_variant_su<U, NT, true>(t.peel_scan_unroll) : peel_variant_su<U, NT, false>(t.peel_scan_unroll);
+}
+
+template <int NT>
+static const void *peel_variant_u(const Tuning &t) {
+    return t.peel_unroll == 8 ? peel_variant_b<8, NT>(t) : peel_variant_b<4, NT>(t);
+}
+
 static const void *peel_variant(const Tuning &t, int *threads) {
     *threads = t.peel_threads;
-    const bool b = t.peel_balanced != 0, u8 = t.peel_unroll == 8;
-    if (t.peel_threads == 256) {
-        if (b) return u8 ? (const void *)peel_kernel<8, 256, true> : (const void *)peel_kernel<4, 256, true>;
-        return u8 ? (const void *)peel_kernel<8, 256, false> : (const void *)peel_kernel<4, 256, false>;
-    }
-    if (b) return u8 ? (const void *)peel_kernel<8, 512, true> : (const void *)peel_kernel<4, 512, true>;
-    return u8 ? (const void *)peel_kernel<8, 512, false> : (const void *)peel_kernel<4, 512, false>;
+    return t.peel_threads == 256 ? peel_variant_u<256>(t) : peel_variant_u<512>(t);
 }
 
 static int peel_grid(const void *kern, int threads, int sm_count, int ctas_per_sm, int *grid) {

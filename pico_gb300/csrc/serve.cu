@@ -407,8 +407,9 @@ int kc_server_submit_decompose(kc_server *S, const int64_t *rowptr, const uint32
     r->n = n;
     r->rowptr.assign(rowptr, rowptr + n + 1);
     r->col.assign(col, col + nnz);
-    // device footprint: CSR, core, batch queues and degrees, with headroom
-    r->need = 3 * (8ull * (n + 1) + 4ull * nnz) + 16ull * n + (1ull << 20);
+    // device footprint: CSR, core, batch queues, degrees and alive lists,
+    // with headroom
+    r->need = 3 * (8ull * (n + 1) + 4ull * nnz) + 24ull * n + (1ull << 20);
     *ticket = submit(S, r);
     return KC_OK;
 }

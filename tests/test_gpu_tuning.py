@@ -26,6 +26,11 @@ SETTINGS = [
     {"peel.balanced": 1, "peel.round_entries": 256, "peel.spill": 0, "peel.steal": 1},
     {"peel.balanced": 1, "peel.round_entries": 1 << 20, "peel.unroll": 8},
     {"peel.balanced": 1, "peel.threads": 256, "peel.chunk": 65536, "peel.queues": 5},
+    {"peel.balanced": 0, "peel.chunk": 256},
+    {"peel.balanced": 0, "peel.unroll": 8, "peel.spill": 0, "peel.steal": 2},
+    {"peel.scan_unroll": 8},
+    {"peel.scan_unroll": 8, "peel.balanced": 1, "peel.chunk": 512, "peel.round_entries": 16384},
+    {"peel.scan_unroll": 8, "peel.threads": 256, "peel.unroll": 8, "peel.spill": 0},
 ]
 
 
