@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <cstdarg>
 #include <cstring>
+#include <mutex>
 #include <string>
 
 #include "kc_device.cuh"
@@ -30,8 +31,48 @@ void clear_error() { g_last_error.clear(); }
 // on the legacy stream and waited for, so the memory is usable from any
 // stream; every caller has finished its own stream's work on a buffer before
 // freeing it.
+//
+// The pool keeps freed memory for reuse instead of returning it to the driver
+// at every synchronisation (its default), so a graph built and freed per
+// request or per step does not remap its buffers each time.  This is a
+// property of this process's pool only.
+static void keep_pool_memory() {
+    static std::mutex mu;
+    static bool done[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return;
+    std::lock_guard<std::mutex> lock(mu);
+    if (done[dev]) return;
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+        uint64_t keep = ~0ull;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    cudaGetLastError();
+    done[dev] = true;
+}
+
+// Free device memory of the current device, counting what this process's pool
+// holds for reuse as free.
+size_t device_free_bytes(size_t *total) {
+    size_t f = 0, t = 0;
+    cudaMemGetInfo(&f, &t);
+    int dev = 0;
+    cudaMemPool_t pool;
+    if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+        uint64_t reserved = 0, used = 0;
+        if (cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &reserved) == cudaSuccess &&
+            cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &used) == cudaSuccess && reserved > used)
+            f += (size_t)(reserved - used);
+    }
+    cudaGetLastError();
+    if (total) *total = t;
+    return f;
+}
+
 int dmalloc(void **p, size_t bytes, const char *what) {
     *p = nullptr;
+    keep_pool_memory();
     cudaError_t e = cudaMallocAsync(p, bytes, cudaStreamLegacy);
     if (e == cudaSuccess) e = cudaStreamSynchronize(cudaStreamLegacy);
     if (e != cudaSuccess) {

@@ -15,6 +15,9 @@ namespace kc {
 
 // Records a formatted message for kc_last_error() and returns `code`.
 int fail(int code, const char *fmt, ...);
+// Free device memory of the current device, including what this process's
+// allocator pool holds for reuse (api.cu).
+size_t device_free_bytes(size_t *total);
 void clear_error();
 
 #define KC_CUDA(call)                                                                          \

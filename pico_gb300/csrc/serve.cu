@@ -8,7 +8,8 @@
 //     submission order on their own lane;
 //   * decompose: the core numbers of a graph sent with the request.  Waiting
 //     requests are admitted as decomposition lanes free up and as device
-//     memory allows (cudaMemGetInfo, minus a reserve and minus what admitted
+//     memory allows (free device memory plus what this process's allocator
+//     pool holds for reuse, minus a reserve and minus what admitted
 //     requests may still allocate); a lane packs every admissible waiting
 //     request (up to a graph count and byte budget) into one segmented CSR
 //     and decomposes them in one batched launch, so requests arriving while
@@ -250,8 +251,8 @@ static void decompose_worker(kc_server *S) {
             for (;;) {
                 if (S->stop && S->dec_q.empty()) return;
                 if (!S->dec_q.empty()) {
-                    size_t free_b = 0, total_b = 0;
-                    cudaMemGetInfo(&free_b, &total_b);
+                    size_t total_b = 0;
+                    const size_t free_b = device_free_bytes(&total_b);
                     const uint64_t avail = free_b > S->cfg.hbm_reserve_bytes + S->admitted_need
                                                ? free_b - S->cfg.hbm_reserve_bytes - S->admitted_need
                                                : 0;
