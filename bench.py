@@ -350,7 +350,8 @@ def run_engine(args, wl, world, rank, local, dist):
         pg.lib().kc_host_free(p)
     g.free()
     if world == 1 and not args.no_batch:
-        line["batched"] = batch_section(pg, device, sptr, args.steps, args.warmup, args.batch_graphs)
+        line["batched"] = batch_section(pg, device, sptr, args.steps, args.warmup, args.batch_graphs,
+                                        not args.no_autotune)
     if world == 1 and not args.no_serve:
         line["serving"] = serve_section(pg, device, args.serve_requests, args.serve_rate)
     if rank == 0:
@@ -362,7 +363,7 @@ BATCH_DESC = ("4096 graphs, n = floor(10^U(2,5)), generator uniform over Erdos-R
               "Barabasi-Albert (m_BA in 1..32), average degree U[4,64], seed 4, packed as one segmented CSR")
 
 
-def batch_section(pg, device, sptr, steps, warmup, num_graphs=4096):
+def batch_section(pg, device, sptr, steps, warmup, num_graphs=4096, autotune=True):
     """Batched (one launch, CUDA graph, autotuned) against the plain form (one
     decomposition call per graph) over the same 4096 graphs; both results are
     compared graph by graph."""
@@ -376,7 +377,7 @@ def batch_section(pg, device, sptr, steps, warmup, num_graphs=4096):
     n, nnz = g.n, g.nnz
     m = nnz // 2
     b = pg.Batch(g, vbase)
-    tuned_ms = b.autotune()
+    tuned_ms = b.autotune() if autotune else None
     for _ in range(warmup):
         b.decompose_device(stream=sptr)
     torch.cuda.synchronize(device)
@@ -418,7 +419,7 @@ def batch_section(pg, device, sptr, steps, warmup, num_graphs=4096):
         "plain_form": "one kc_decompose(KC_PEELONE_DYN) call per graph over the same device-resident graphs",
         "batched_over_plain": round(plain_ms / batched_ms, 2), "identical_results": same,
         "autotuned": {"batch.small_n": kb, "batch.small_threads": kp, "batch.chunk": kc,
-                      "best_ms": round(tuned_ms, 4)},
+                      "best_ms": round(tuned_ms, 4) if tuned_ms is not None else None},
         "generate_s": round(gen_s, 2),
     }
 
@@ -484,6 +485,7 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the 4096-graph batched-vs-plain section")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving section")
     ap.add_argument("--batch-graphs", type=int, default=4096, help="graphs in the batched section")
+    ap.add_argument("--no-autotune", action="store_true", help="batched section: keep the default configuration")
     ap.add_argument("--serve-requests", type=int, default=40)
     ap.add_argument("--serve-rate", type=float, default=20.0, help="Poisson arrival rate, requests/s")
     args = ap.parse_args()
