@@ -21,7 +21,7 @@ def test_abi_version_and_error_string():
 
 def test_no_gpu_fails_loudly_not_silently():
     if pg.device_count() > 0:
-        return  # on a GPU machine this path is covered by the gpu tests
+        return  # with a GPU present this path is covered by the gpu tests
     try:
         pg.Graph.from_edges([0, 1], [1, 2], 3)
     except pg.KCoreError as e:
