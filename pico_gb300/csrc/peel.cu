@@ -430,22 +430,28 @@ __global__ void __launch_bounds__(NT, 1024 / NT) peel_kernel(PeelArgs A) {
 #pragma unroll
                 for (int k = 0; k < SCAN_U; k++) d[k] = inr[k] ? __ldcg(&A.deg[v[k]]) : 0u;
                 unsigned dkeep = NO_LEVEL;
+                // claims: lanes whose vertices share a bitmap word set their
+                // bits with one atomicOr by the lowest such lane; all the
+                // atomics are issued before any result is used
+                unsigned oldw[SCAN_U];
+                int leader[SCAN_U];
 #pragma unroll
                 for (int k = 0; k < SCAN_U; k++) {
                     keep[k] = inr[k] && (int)d[k] > (int)L;
                     if (keep[k]) dkeep = min(dkeep, d[k]);
-                    // claims: lanes whose vertices share a bitmap word set their
-                    // bits with one atomicOr by the lowest such lane
                     const bool want = inr[k] && !keep[k];
                     const unsigned word = want ? (v[k] >> 5) : 0xffffffffu;
                     const unsigned bit = want ? (1u << (v[k] & 31)) : 0u;
                     const unsigned peers = __match_any_sync(KC_FULL_MASK, word);
                     const unsigned bits = __reduce_or_sync(peers, bit);
-                    const int leader = __ffs(peers) - 1;
-                    unsigned old = 0;
-                    if (want && (int)lane == leader) old = atomicOr(&A.claimed[word], bits);
-                    old = __shfl_sync(KC_FULL_MASK, old, leader);
-                    take[k] = want && !(old & bit);
+                    leader[k] = __ffs(peers) - 1;
+                    oldw[k] = 0;
+                    if (want && (int)lane == leader[k]) oldw[k] = atomicOr(&A.claimed[word], bits);
+                }
+#pragma unroll
+                for (int k = 0; k < SCAN_U; k++) {
+                    const unsigned old = __shfl_sync(KC_FULL_MASK, oldw[k], leader[k]);
+                    take[k] = inr[k] && !keep[k] && !(old & (1u << (v[k] & 31)));
                 }
                 dkeep = __reduce_min_sync(KC_FULL_MASK, dkeep);
                 if (lane == 0 && dkeep != NO_LEVEL) atomicMin(&min_sh, dkeep);
@@ -453,8 +459,9 @@ __global__ void __launch_bounds__(NT, 1024 / NT) peel_kernel(PeelArgs A) {
                 unsigned any_take = 0;
 #pragma unroll
                 for (int k = 0; k < SCAN_U; k++) {
-                    // a claimed vertex with an empty row needs no processing
-                    push[k] = take[k] && (A.rowptr[v[k] + 1] != A.rowptr[v[k]]);
+                    // listed vertices have non-empty rows (the degree-0 ones
+                    // are peeled by peel_init), so every claim is queued
+                    push[k] = take[k];
                     kb[k] = __ballot_sync(KC_FULL_MASK, keep[k]);
                     cb[k] = __ballot_sync(KC_FULL_MASK, push[k]);
                     const unsigned tb = __ballot_sync(KC_FULL_MASK, take[k]);
@@ -645,20 +652,25 @@ __global__ void __launch_bounds__(NT, 1024 / NT) peel_kernel(PeelArgs A) {
                     }
 #pragma unroll
                     for (int k = 0; k < PEEL_U; k++) a[k] = live[k] ? atomicSub(&A.deg[u[k]], 1u) : 0u;
+                    // the decrement that moved u from L+1 to L claims it; the
+                    // claim atomics of all PEEL_U entries are in flight together
+                    unsigned oldc[PEEL_U];
 #pragma unroll
                     for (int k = 0; k < PEEL_U; k++) {
-                        bool push = false;
+                        oldc[k] = ~0u;
                         if (live[k]) {
                             if (a[k] == L + 1) {
-                                const unsigned bit = 1u << (u[k] & 31);
-                                unsigned old = atomicOr(&A.claimed[u[k] >> 5], bit);
-                                push = !(old & bit);
+                                oldc[k] = atomicOr(&A.claimed[u[k] >> 5], 1u << (u[k] & 31));
                             } else if ((int)a[k] <= (int)L) {
                                 atomicAdd(&A.deg[u[k]], 1u);
                             } else {
                                 local_min = min(local_min, a[k] - 1);
                             }
                         }
+                    }
+#pragma unroll
+                    for (int k = 0; k < PEEL_U; k++) {
+                        const bool push = !(oldc[k] & (1u << (u[k] & 31)));
                         unsigned pb = __ballot_sync(KC_FULL_MASK, push);
                         wclaims += __popc(pb);
                         if (pb) {

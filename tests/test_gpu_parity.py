@@ -222,3 +222,24 @@ def test_config3_rmat25_planted_core():
     assert st.kmax == kmax and kmax >= 2000  # the planted core dominates
     got_h, _ = g.decompose("NbrCore")
     assert np.array_equal(got_h, core)
+
+
+def test_relabelling_and_local_core_property():
+    """Relabelling the vertices permutes the core numbers, and the result
+    passes the local k-core check (each vertex of core k has at least k
+    neighbours of core >= k and is not in the (k+1)-core)."""
+    rng = np.random.default_rng(17)
+    g = pg.rmat_graph(15, 16, seed=9)
+    rp, col = g.csr()
+    n = g.n
+    core, _ = g.decompose("peelone_dyn")
+    assert oracle.check_local(rp, col, core) == 0
+    perm = rng.permutation(n).astype(np.uint32)
+    src = np.repeat(np.arange(n, dtype=np.uint32), np.diff(rp))
+    h = pg.Graph.from_edges(perm[src], perm[col], n, dedup=True)
+    for method in ("peelone_dyn", "histo", "gppeel"):
+        c2, _ = h.decompose(method)
+        want = np.where(np.diff(rp) == 0, 1, core) if method == "gppeel" else core
+        assert np.array_equal(c2[perm], want), method
+    g.free()
+    h.free()
