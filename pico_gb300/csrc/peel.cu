@@ -168,7 +168,8 @@ __global__ void __launch_bounds__(NT, 1024 / NT) peel_kernel(PeelArgs A) {
     __shared__ unsigned int steal_cnt, probe, claims_sh, spill_rr;
     __shared__ unsigned int level_sh, li_sh;
     __shared__ unsigned long long wait_t0;
-    __shared__ unsigned int warp_cnt[SCAN_U][PEEL_WARPS];
+    __shared__ unsigned int warp_cnt[SCAN_U][PEEL_WARPS];   // scan: survivors per warp
+    __shared__ unsigned int warp_push[SCAN_U][PEEL_WARPS];  // scan: claims per warp
     __shared__ unsigned long long next_tile;
     __shared__ unsigned int withheld;
     __shared__ unsigned int rounds_sh;
@@ -448,50 +449,58 @@ __global__ void __launch_bounds__(NT, 1024 / NT) peel_kernel(PeelArgs A) {
                     oldw[k] = 0;
                     if (want && (int)lane == leader[k]) oldw[k] = atomicOr(&A.claimed[word], bits);
                 }
+                dkeep = __reduce_min_sync(KC_FULL_MASK, dkeep);
+                if (lane == 0 && dkeep != NO_LEVEL) atomicMin(&min_sh, dkeep);
+                // survivors first: their count reserves space in the next list
+                // while the claim atomics are still in flight
+                unsigned kb[SCAN_U], cb[SCAN_U];
+#pragma unroll
+                for (int k = 0; k < SCAN_U; k++) {
+                    kb[k] = __ballot_sync(KC_FULL_MASK, keep[k]);
+                    if (lane == 0) warp_cnt[k][warp] = __popc(kb[k]);
+                }
+                __syncthreads();
+                // offsets: sub-tiles in order, warps in order within a sub-tile
+                unsigned ktot = 0;
+                unsigned kofs[SCAN_U];
+#pragma unroll
+                for (int k = 0; k < SCAN_U; k++) {
+                    kofs[k] = ktot;
+                    for (unsigned w2 = 0; w2 < PEEL_WARPS; w2++) {
+                        const unsigned x = warp_cnt[k][w2];
+                        if (w2 < warp) kofs[k] += x;
+                        ktot += x;
+                    }
+                }
+                if (tid == 0 && ktot) out_base = atomicAdd(&ctl->out_len[s], (unsigned long long)ktot);
+                unsigned any_take = 0;
 #pragma unroll
                 for (int k = 0; k < SCAN_U; k++) {
                     const unsigned old = __shfl_sync(KC_FULL_MASK, oldw[k], leader[k]);
                     take[k] = inr[k] && !keep[k] && !(old & (1u << (v[k] & 31)));
-                }
-                dkeep = __reduce_min_sync(KC_FULL_MASK, dkeep);
-                if (lane == 0 && dkeep != NO_LEVEL) atomicMin(&min_sh, dkeep);
-                unsigned kb[SCAN_U], cb[SCAN_U];
-                unsigned any_take = 0;
-#pragma unroll
-                for (int k = 0; k < SCAN_U; k++) {
                     // listed vertices have non-empty rows (the degree-0 ones
                     // are peeled by peel_init), so every claim is queued
                     push[k] = take[k];
-                    kb[k] = __ballot_sync(KC_FULL_MASK, keep[k]);
                     cb[k] = __ballot_sync(KC_FULL_MASK, push[k]);
-                    const unsigned tb = __ballot_sync(KC_FULL_MASK, take[k]);
-                    any_take += __popc(tb);
-                    if (lane == 0) warp_cnt[k][warp] = __popc(kb[k]) | (__popc(cb[k]) << 16);
+                    any_take += __popc(cb[k]);
+                    if (lane == 0) warp_push[k][warp] = __popc(cb[k]);
                 }
                 if (lane == 0 && any_take) {
                     claimed_any = 1;
                     if (A.trace) atomicAdd(&claims_sh, any_take);
                 }
                 __syncthreads();
-                // offsets: sub-tiles in order, warps in order within a sub-tile
-                unsigned ktot = 0, ctot = 0;
-                unsigned kofs[SCAN_U], cofs[SCAN_U];
+                unsigned ctot = 0;
+                unsigned cofs[SCAN_U];
 #pragma unroll
                 for (int k = 0; k < SCAN_U; k++) {
-                    kofs[k] = ktot;
                     cofs[k] = ctot;
                     for (unsigned w2 = 0; w2 < PEEL_WARPS; w2++) {
-                        unsigned x = warp_cnt[k][w2];
-                        if (w2 < warp) {
-                            kofs[k] += x & 0xffffu;
-                            cofs[k] += x >> 16;
-                        }
-                        ktot += x & 0xffffu;
-                        ctot += x >> 16;
+                        const unsigned x = warp_push[k][w2];
+                        if (w2 < warp) cofs[k] += x;
+                        ctot += x;
                     }
                 }
-                if (tid == 0 && ktot) out_base = atomicAdd(&ctl->out_len[s], (unsigned long long)ktot);
-                __syncthreads();
                 const unsigned lt = (1u << lane) - 1u;
 #pragma unroll
                 for (int k = 0; k < SCAN_U; k++) {
@@ -734,9 +743,12 @@ __global__ void __launch_bounds__(NT, 1024 / NT) peel_kernel(PeelArgs A) {
         if (tid == 0) {
             unsigned nxt = NO_LEVEL;
             if (mode == M_DONE) {
+                // pending reached zero (read with acquire) after every CTA's
+                // last update of this slot: both values are final and are
+                // fetched together
                 __threadfence();
-                nxt = ld_acquire(&ctl->next_min[s]);
-                scan_len = ld_acquire64(&ctl->out_len[s]);
+                nxt = ld_relaxed(&ctl->next_min[s]);
+                scan_len = ld_relaxed64(&ctl->out_len[s]);
                 if (blockIdx.x == 0) {
                     ctl->level_indices = li + 1;
                     if (ld_relaxed(&ctl->nonempty[s])) ctl->levels += 1;
