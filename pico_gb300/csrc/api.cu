@@ -267,7 +267,9 @@ static int from_csr_common(const int64_t *rowptr, const uint32_t *col, uint32_t 
     kc_graph *g = nullptr;
     KC_TRY(new_graph(device, &g));
     int64_t nnz = 0;
-    cudaError_t e = cudaMemcpy(&nnz, rowptr + n, 8, kind == cudaMemcpyHostToDevice ? cudaMemcpyHostToHost : cudaMemcpyDeviceToHost);
+    cudaError_t e = cudaSuccess;
+    if (kind == cudaMemcpyHostToDevice) memcpy(&nnz, rowptr + n, 8);  // host memory: no driver call
+    else e = cudaMemcpy(&nnz, rowptr + n, 8, cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) { delete g; return fail(KC_ERR_CUDA, "read rowptr[n]: %s", cudaGetErrorString(e)); }
     if (nnz < 0 || (nnz > 0 && !col)) { delete g; return fail(KC_ERR_INVALID, "bad rowptr[n] = %lld", (long long)nnz); }
     g->n = n;
