@@ -274,7 +274,9 @@ typedef struct kc_batch kc_batch;
 int kc_batch_create(kc_graph *g, const uint32_t *vbase, uint32_t num_graphs, kc_batch **out);
 /* Parameters: "batch.small_n" (largest graph, in vertices, of the small-CTA
  * class), "batch.small_threads", "batch.large_threads", "batch.chunk" (row
- * entries per work item), "batch.cuda_graph" (1 = capture once, replay),
+ * entries per work item), "batch.large_shared" (1 = graphs above small_n
+ * keep degrees in shared memory, one CTA per SM; 0 = in global memory, as many
+ * CTAs per SM as fit), "batch.cuda_graph" (1 = capture once, replay),
  * "trace" (1 = record per-graph timings, see kc_batch_trace). */
 int kc_batch_set_param(kc_batch *b, const char *name, int64_t value);
 int kc_batch_get_param(const kc_batch *b, const char *name, int64_t *value);

@@ -334,6 +334,7 @@ struct BatchConfig {
     int small_threads = 256;
     int large_threads = 1024;
     uint32_t chunk = 256;
+    int large_shared = 1;  // 0: graphs above small_n keep their degrees in global memory (more CTAs per SM)
 };
 
 struct BatchClass {
@@ -416,6 +417,7 @@ static int plan(kc_batch *b) {
         const bool fits16 = b->maxdeg[i] < 65535u;
         int k;
         if (fits16 && n <= small_n) k = 0;
+        else if (!b->cfg.large_shared) k = 3;
         else if (fits16 && n <= large_u16) k = 1;
         else if (n <= large_u32) k = 2;
         else k = 3;
@@ -638,6 +640,8 @@ int kc_batch_set_param(kc_batch *b, const char *name, int64_t value) {
         if (value < BATCH_MIN_CHUNK || value > (1 << 16) || (value & (value - 1)))
             return fail(KC_ERR_INVALID, "batch.chunk: power of two in [%u, 2^16]", BATCH_MIN_CHUNK);
         b->cfg.chunk = (uint32_t)value;
+    } else if (k == "batch.large_shared") {
+        b->cfg.large_shared = value ? 1 : 0;
     } else if (k == "batch.cuda_graph") {
         b->use_graph = value != 0;
         return KC_OK;
@@ -665,6 +669,7 @@ int kc_batch_get_param(const kc_batch *b, const char *name, int64_t *value) {
     else if (k == "batch.small_threads") *value = b->cfg.small_threads;
     else if (k == "batch.large_threads") *value = b->cfg.large_threads;
     else if (k == "batch.chunk") *value = b->cfg.chunk;
+    else if (k == "batch.large_shared") *value = b->cfg.large_shared;
     else if (k == "batch.cuda_graph") *value = b->use_graph ? 1 : 0;
     else return fail(KC_ERR_INVALID, "unknown parameter %s", name);
     return KC_OK;

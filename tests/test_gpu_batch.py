@@ -85,3 +85,22 @@ def test_config4_batch_mix_4096():
     rp, col = g.csr()
     core, _ = oracle.bz(rp, col)
     assert np.array_equal(got, core)
+
+
+@pytest.mark.parametrize("large_threads", [256, 1024])
+def test_large_graphs_in_global_memory(large_threads):
+    """Graphs above batch.small_n with their degrees in global memory (many
+    CTAs per SM) give the same core numbers as the shared-memory class."""
+    g, vbase, _ = workloads.batch_mix(96, seed=11)
+    b = pg.Batch(g, vbase)
+    b.set_param("batch.small_n", 2048)
+    want, _ = b.decompose()
+    b.set_param("batch.large_shared", 0)
+    b.set_param("batch.large_threads", large_threads)
+    got, _ = b.decompose()
+    assert b.get_param("batch.large_shared") == 0
+    assert np.array_equal(got, want)
+    rp, col = g.csr()
+    assert np.array_equal(got, oracle.bz(rp, col)[0])
+    b.free()
+    g.free()
