@@ -91,7 +91,7 @@ struct Tuning {
     int peel_round_entries = 16384;
     int peel_scan_unroll = 4;  // alive-list entries per thread per scan tile: 4 or 8
     int trace = 0;
-    int64_t update_incremental_max = 65536;  // larger update batches: full recompute
+    int64_t update_incremental_max = 512;  // larger update batches: full recompute (measured crossover ~1000 edges)
     int64_t wait_timeout_us = 2000000;       // limit of one inter-CTA wait
     int withhold = 0;  // failure-detection hook: one CTA never signals, so the others' waits run out
 };

@@ -49,7 +49,30 @@ __device__ __forceinline__ uint32_t lower_bound_u32(const uint32_t *a, uint32_t 
 // Phase 1, one warp per row with changes: the positions (in the old row) of
 // entries to delete and the values to insert, each sorted, and the new row
 // length.  A pair both deleted and inserted stays as it is.
-__global__ void merge_plan(const int64_t *__restrict__ rowptr, const uint32_t *__restrict__ col, uint32_t n,
+// Every row: new length = old length, no changes yet; flags the rows that
+// the change lists touch.
+__global__ void mark_changed(const int64_t *__restrict__ rowptr, uint32_t n, const int64_t *__restrict__ drp,
+                             const int64_t *__restrict__ irp, uint32_t *dcnt, uint32_t *icnt, uint32_t *newlen,
+                             uint32_t *flag) {
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n; v += (uint64_t)gridDim.x * blockDim.x) {
+        newlen[v] = (uint32_t)(rowptr[v + 1] - rowptr[v]);
+        if (dcnt) dcnt[v] = 0;
+        if (icnt) icnt[v] = 0;
+        const bool ch = (drp && drp[v + 1] != drp[v]) || (irp && irp[v + 1] != irp[v]);
+        flag[v] = ch ? 1u : 0u;
+    }
+}
+
+__global__ void list_changed(const uint32_t *__restrict__ flag, const int64_t *__restrict__ pos, uint32_t n,
+                             uint32_t *changed) {
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n; v += (uint64_t)gridDim.x * blockDim.x)
+        if (flag[v]) changed[pos[v]] = (uint32_t)v;
+}
+
+// Plans the changed rows (one warp per listed row): positions of deleted
+// entries, inserted values not already present, new row lengths.
+__global__ void merge_plan(const int64_t *__restrict__ rowptr, const uint32_t *__restrict__ col,
+                           const uint32_t *__restrict__ changed, uint32_t nchanged,
                            const int64_t *__restrict__ drp, const uint32_t *__restrict__ dcol,
                            const int64_t *__restrict__ irp, const uint32_t *__restrict__ icol, uint32_t *dpos,
                            uint32_t *dcnt, uint32_t *ival, uint32_t *icnt, uint32_t *newlen,
@@ -58,7 +81,8 @@ __global__ void merge_plan(const int64_t *__restrict__ rowptr, const uint32_t *_
     const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
     const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
     unsigned long long nd = 0, ni = 0;
-    for (uint64_t v = warp; v < n; v += nw) {
+    for (uint64_t ci = warp; ci < nchanged; ci += nw) {
+        const uint32_t v = changed[ci];
         const int64_t r0 = rowptr[v];
         const uint32_t len = (uint32_t)(rowptr[v + 1] - r0);
         const int64_t d0 = drp ? drp[v] : 0, i0 = irp ? irp[v] : 0;
@@ -119,7 +143,48 @@ __global__ void merge_plan(const int64_t *__restrict__ rowptr, const uint32_t *_
 }
 
 // Phase 2, one warp per row: write the merged, sorted row.
-__global__ void merge_write(const int64_t *__restrict__ rowptr, const uint32_t *__restrict__ col, uint32_t n,
+// Runs of unchanged rows between consecutive changed rows: run j covers
+// rows changed[j-1]+1 .. changed[j]-1 (changed[-1] = -1, changed[R] = n);
+// its old entries [ra, rb) move by rd.
+__global__ void make_runs(const int64_t *__restrict__ rowptr, const int64_t *__restrict__ nrow,
+                          const uint32_t *__restrict__ changed, uint32_t R, uint32_t n, int64_t *ra, int64_t *rb,
+                          int64_t *rd) {
+    for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j <= R; j += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t first = j ? changed[j - 1] + 1 : 0u;
+        const uint32_t end = j < R ? changed[j] : n;
+        ra[j] = rowptr[first];
+        rb[j] = rowptr[end > first ? end : first];
+        rd[j] = nrow[first] - rowptr[first];
+    }
+}
+
+// Bulk move of the unchanged rows: each CTA copies one tile of the old column
+// array, run by run (runs are ordered and usually span many tiles).
+constexpr uint64_t RUN_TILE = 8192;
+__global__ void copy_runs(const uint32_t *__restrict__ col, uint64_t nnz_old, const int64_t *__restrict__ ra,
+                          const int64_t *__restrict__ rb, const int64_t *__restrict__ rd, uint32_t R,
+                          uint32_t *ncol) {
+    for (uint64_t t0 = blockIdx.x * RUN_TILE; t0 < nnz_old; t0 += (uint64_t)gridDim.x * RUN_TILE) {
+        const uint64_t t1 = t0 + RUN_TILE < nnz_old ? t0 + RUN_TILE : nnz_old;
+        // first run ending after t0
+        uint32_t lo = 0, hi = R + 1;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if ((uint64_t)rb[mid] <= t0) lo = mid + 1;
+            else hi = mid;
+        }
+        for (uint32_t j = lo; j <= R && (uint64_t)ra[j] < t1; j++) {
+            const uint64_t a = (uint64_t)ra[j] > t0 ? (uint64_t)ra[j] : t0;
+            const uint64_t b = (uint64_t)rb[j] < t1 ? (uint64_t)rb[j] : t1;
+            const int64_t d = rd[j];
+            for (uint64_t e = a + threadIdx.x; e < b; e += blockDim.x) ncol[(int64_t)e + d] = col[e];
+        }
+    }
+}
+
+// Writes the changed rows (one warp per listed row).
+__global__ void merge_write(const int64_t *__restrict__ rowptr, const uint32_t *__restrict__ col,
+                            const uint32_t *__restrict__ changed, uint32_t nchanged,
                             const int64_t *__restrict__ drp, const uint32_t *__restrict__ dpos,
                             const uint32_t *__restrict__ dcnt, const int64_t *__restrict__ irp,
                             const uint32_t *__restrict__ ival, const uint32_t *__restrict__ icnt,
@@ -127,7 +192,8 @@ __global__ void merge_write(const int64_t *__restrict__ rowptr, const uint32_t *
     const unsigned lane = threadIdx.x & 31;
     const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
     const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-    for (uint64_t v = warp; v < n; v += nw) {
+    for (uint64_t ci = warp; ci < nchanged; ci += nw) {
+        const uint32_t v = changed[ci];
         const int64_t r0 = rowptr[v];
         const uint32_t len = (uint32_t)(rowptr[v + 1] - r0);
         const int64_t w0 = nrow[v];
@@ -284,22 +350,53 @@ static int apply_changes(Graph *g, const uint32_t *d_isrc, const uint32_t *d_ids
     }
     KC_TRY(sc.get(&newlen, n, "new row lengths"));
     KC_TRY(sc.get(&applied, 2, "applied counts"));
+    uint32_t *flag = nullptr;
+    int64_t *cpos = nullptr;
+    KC_TRY(sc.get(&flag, n, "changed-row flags"));
+    KC_TRY(sc.get(&cpos, (uint64_t)n + 1, "changed-row positions"));
     KC_CUDA(cudaMemsetAsync(applied, 0, 16, s));
-    const int gw = grid_of(g, (uint64_t)n * 32);
-    merge_plan<<<gw, 256, 0, s>>>(g->rowptr, g->col, n, md ? dg.rowptr : nullptr, md ? dg.col : nullptr,
-                                  mi ? ig.rowptr : nullptr, mi ? ig.col : nullptr, dpos, dcnt, ival, icnt, newlen,
-                                  applied);
+    const int64_t *drp = md ? dg.rowptr : nullptr, *irp = mi ? ig.rowptr : nullptr;
+    // only the rows that the change lists touch are planned and rewritten
+    // row by row; the others move as whole runs
+    mark_changed<<<grid_of(g, n), 256, 0, s>>>(g->rowptr, n, drp, irp, dcnt, icnt, newlen, flag);
+    KC_TRY(exclusive_scan_u32_i64(flag, cpos, n, s));
+    int64_t R64 = 0;
+    KC_CUDA(cudaMemcpyAsync(&R64, cpos + n, 8, cudaMemcpyDeviceToHost, s));
+    KC_CUDA(cudaStreamSynchronize(s));
+    const uint32_t R = (uint32_t)R64;
+    uint32_t *changed = nullptr;
+    int64_t *ra = nullptr, *rb = nullptr, *rd = nullptr;
+    KC_TRY(sc.get(&changed, (uint64_t)R + 1, "changed rows"));
+    KC_TRY(sc.get(&ra, (uint64_t)R + 1, "run starts"));
+    KC_TRY(sc.get(&rb, (uint64_t)R + 1, "run ends"));
+    KC_TRY(sc.get(&rd, (uint64_t)R + 1, "run shifts"));
+    list_changed<<<grid_of(g, n), 256, 0, s>>>(flag, cpos, n, changed);
+    const int gw = grid_of(g, (uint64_t)std::max<uint32_t>(R, 1) * 32);
+    if (R)
+        merge_plan<<<gw, 256, 0, s>>>(g->rowptr, g->col, changed, R, drp, md ? dg.col : nullptr, irp,
+                                      mi ? ig.col : nullptr, dpos, dcnt, ival, icnt, newlen, applied);
     int64_t *rp_new = nullptr;
     KC_TRY(dalloc(&rp_new, (uint64_t)n + 1, "row offsets"));
     int rc = exclusive_scan_u32_i64(newlen, rp_new, n, s);
     int64_t nnz_new = 0;
     if (!rc) {
-        cudaMemcpy(&nnz_new, rp_new + n, 8, cudaMemcpyDeviceToHost);
+        cudaMemcpyAsync(&nnz_new, rp_new + n, 8, cudaMemcpyDeviceToHost, s);
+        cudaError_t e0 = cudaStreamSynchronize(s);
+        if (e0 != cudaSuccess) rc = fail(KC_ERR_CUDA, "CSR merge plan: %s", cudaGetErrorString(e0));
+    }
+    if (!rc) {
         uint32_t *col_new = nullptr;
         rc = dalloc(&col_new, (uint64_t)nnz_new + 1, "column ids");
         if (!rc) {
-            merge_write<<<gw, 256, 0, s>>>(g->rowptr, g->col, n, md ? dg.rowptr : nullptr, dpos, dcnt,
-                                           mi ? ig.rowptr : nullptr, ival, icnt, rp_new, col_new);
+            make_runs<<<grid_of(g, (uint64_t)R + 1), 256, 0, s>>>(g->rowptr, rp_new, changed, R, n, ra, rb, rd);
+            if (g->nnz) {
+                const uint64_t tiles = (g->nnz + RUN_TILE - 1) / RUN_TILE;
+                const int cb = (int)std::min<uint64_t>(tiles, (uint64_t)g->sm_count * 16);
+                copy_runs<<<cb, 256, 0, s>>>(g->col, g->nnz, ra, rb, rd, R, col_new);
+            }
+            if (R)
+                merge_write<<<gw, 256, 0, s>>>(g->rowptr, g->col, changed, R, drp, dpos, dcnt, irp, ival, icnt, rp_new,
+                                               col_new);
             unsigned long long h[2];
             cudaMemcpyAsync(h, applied, 16, cudaMemcpyDeviceToHost, s);
             cudaError_t e = cudaStreamSynchronize(s);
