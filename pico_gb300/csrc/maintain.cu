@@ -222,11 +222,41 @@ __global__ void merge_write(const int64_t *__restrict__ rowptr, const uint32_t *
 }
 
 // Rows sorted and without repeated neighbours (required by the merge).
+// Counts entries that are not strictly above their predecessor in the same
+// row.  Each CTA checks one tile of entries; the row starts falling in the
+// tile are marked in shared memory first, so hub rows split over many CTAs.
+constexpr uint64_t CHECK_TILE = 8192;
 __global__ void rows_simple(const int64_t *__restrict__ rowptr, const uint32_t *__restrict__ col, uint32_t n,
-                            unsigned long long *bad) {
+                            uint64_t nnz, unsigned long long *bad) {
+    __shared__ uint32_t starts[CHECK_TILE / 32];
+    __shared__ uint32_t first_row;
     unsigned long long b = 0;
-    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n; v += (uint64_t)gridDim.x * blockDim.x)
-        for (int64_t e = rowptr[v] + 1; e < rowptr[v + 1]; e++) b += col[e] <= col[e - 1];
+    for (uint64_t t0 = blockIdx.x * CHECK_TILE; t0 < nnz; t0 += (uint64_t)gridDim.x * CHECK_TILE) {
+        const uint64_t t1 = t0 + CHECK_TILE < nnz ? t0 + CHECK_TILE : nnz;
+        for (unsigned i = threadIdx.x; i < CHECK_TILE / 32; i += blockDim.x) starts[i] = 0;
+        if (threadIdx.x == 0) {
+            // the last row starting at or before t0
+            uint32_t lo = 0, hi = n;
+            while (lo < hi) {
+                const uint32_t mid = (lo + hi + 1) >> 1;
+                if ((uint64_t)rowptr[mid] <= t0) lo = mid;
+                else hi = mid - 1;
+            }
+            first_row = lo;
+        }
+        __syncthreads();
+        for (uint64_t v = first_row + threadIdx.x; v < n && (uint64_t)rowptr[v] < t1; v += blockDim.x) {
+            const uint64_t r = (uint64_t)rowptr[v];
+            if (r >= t0) atomicOr(&starts[(r - t0) >> 5], 1u << ((r - t0) & 31));
+        }
+        __syncthreads();
+        for (uint64_t e = t0 + threadIdx.x; e < t1; e += blockDim.x) {
+            const uint64_t o = e - t0;
+            const bool is_start = (starts[o >> 5] >> (o & 31)) & 1u;
+            if (!is_start && e > 0) b += col[e] <= col[e - 1];
+        }
+        __syncthreads();
+    }
     if (b) atomicAdd(bad, b);
 }
 
@@ -480,7 +510,11 @@ int graph_update(Graph *g, const uint32_t *ins_src, const uint32_t *ins_dst, uin
         unsigned long long *bad = nullptr;
         KC_TRY(dalloc(&bad, 1, "row check"));
         cudaMemsetAsync(bad, 0, 8, s);
-        if (n) rows_simple<<<grid_of(g, n), 256, 0, s>>>(g->rowptr, g->col, n, bad);
+        if (n && g->nnz) {
+            const uint64_t tiles = (g->nnz + CHECK_TILE - 1) / CHECK_TILE;
+            rows_simple<<<(int)std::min<uint64_t>(tiles, (uint64_t)g->sm_count * 16), 256, 0, s>>>(g->rowptr, g->col, n,
+                                                                                                   g->nnz, bad);
+        }
         unsigned long long hb = 0;
         cudaMemcpyAsync(&hb, bad, 8, cudaMemcpyDeviceToHost, s);
         cudaError_t e = cudaStreamSynchronize(s);
