@@ -79,7 +79,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
             objs.append(obj)
     if _stale(LIB, objs):
         tmp = LIB + ".tmp%d" % os.getpid()
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lpthread"]
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lpthread", "-ldl"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed: %s\n%s\n%s" % (" ".join(cmd), r.stdout, r.stderr))

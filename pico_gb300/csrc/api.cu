@@ -196,6 +196,7 @@ void kc_host_free_edges(uint32_t *src, uint32_t *dst) {
 int kc_graph_from_edges_device(const uint32_t *d_src, const uint32_t *d_dst, uint64_t m, uint32_t n, uint32_t flags,
                                int device, kc_graph **out) {
     clear_error();
+    NvtxRange nvtx_("kc_graph_from_edges_device");
     if (!out || (m && (!d_src || !d_dst))) return fail(KC_ERR_INVALID, "null argument");
     *out = nullptr;
     kc_graph *g = nullptr;
@@ -251,6 +252,7 @@ int kc_graph_from_edges(const uint32_t *src, const uint32_t *dst, uint64_t m, ui
 
 int kc_graph_from_mtx(const char *path, int mode, int device, kc_graph **out) {
     clear_error();
+    NvtxRange nvtx_("kc_graph_from_mtx");
     uint32_t n = 0, *src = nullptr, *dst = nullptr;
     uint64_t m = 0;
     KC_TRY(parse_mtx(path, mode, &n, &m, &src, &dst));
@@ -262,6 +264,7 @@ int kc_graph_from_mtx(const char *path, int mode, int device, kc_graph **out) {
 
 static int from_csr_common(const int64_t *rowptr, const uint32_t *col, uint32_t n, int device, kc_graph **out,
                            cudaMemcpyKind kind) {
+    NvtxRange nvtx_("kc_graph_from_csr");
     if (!out || !rowptr) return fail(KC_ERR_INVALID, "null argument");
     *out = nullptr;
     kc_graph *g = nullptr;
@@ -415,6 +418,7 @@ int kc_graph_virtual_layout(kc_graph *g, uint32_t part_size, uint32_t *node_poin
 
 int kc_decompose(kc_graph *g, int method, uint32_t *core_out, int out_on_device, kc_stats *stats, void *stream) {
     clear_error();
+    NvtxRange nvtx_("kc_decompose");
     if (!g) return fail(KC_ERR_INVALID, "null graph");
     if (method < KC_HISTO || method > KC_AUTO) return fail(KC_ERR_INVALID, "unknown method %d", method);
     KC_CUDA(cudaSetDevice(g->device));
@@ -536,6 +540,7 @@ int kc_graph_update(kc_graph *g, const uint32_t *ins_src, const uint32_t *ins_ds
                     const uint32_t *del_src, const uint32_t *del_dst, uint64_t n_del, uint32_t *core_out,
                     int out_on_device, kc_update_stats *stats) {
     clear_error();
+    NvtxRange nvtx_("kc_graph_update");
     if (!g || (n_ins && (!ins_src || !ins_dst)) || (n_del && (!del_src || !del_dst)))
         return fail(KC_ERR_INVALID, "null argument");
     KC_CUDA(cudaSetDevice(g->device));

@@ -677,6 +677,7 @@ int kc_batch_get_param(const kc_batch *b, const char *name, int64_t *value) {
 
 int kc_batch_decompose(kc_batch *b, uint32_t *core_out, int out_on_device, kc_stats *stats, void *stream) {
     clear_error();
+    NvtxRange nvtx_("kc_batch_decompose");
     if (!b) return fail(KC_ERR_INVALID, "null batch");
     Graph *g = b->g;
     KC_CUDA(cudaSetDevice(g->device));
@@ -708,6 +709,7 @@ int kc_batch_decompose(kc_batch *b, uint32_t *core_out, int out_on_device, kc_st
 
 int kc_batch_autotune(kc_batch *b, double *best_ms) {
     clear_error();
+    NvtxRange nvtx_("kc_batch_autotune");
     if (!b) return fail(KC_ERR_INVALID, "null batch");
     KC_CUDA(cudaSetDevice(b->g->device));
     const BatchConfig keep = b->cfg;

@@ -1,6 +1,7 @@
 // Internal declarations shared by the translation units of libkcore.so.
 #pragma once
 
+#include <nvtx3/nvToolsExt.h>
 #include <cuda_runtime.h>
 
 #include <cstdarg>
@@ -15,6 +16,15 @@ namespace kc {
 
 // Records a formatted message for kc_last_error() and returns `code`.
 int fail(int code, const char *fmt, ...);
+
+// Named range on profiler timelines (NVTX), open for the lifetime of the
+// object; free when no profiler is attached.
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
 // Free device memory of the current device, including what this process's
 // allocator pool holds for reuse (api.cu).
 size_t device_free_bytes(size_t *total);

@@ -155,6 +155,7 @@ static void update_worker(kc_server *S) {
         }
         r->t_start = Clock::now();
         Graph *g = S->g;
+        NvtxRange nvtx_("server update request");
         int rc = graph_update(g, r->is.data(), r->id.data(), r->is.size(), r->ds.data(), r->dd.data(), r->ds.size(),
                               &r->ust);
         if (rc == KC_OK) {
@@ -294,7 +295,11 @@ static void decompose_worker(kc_server *S) {
         }
         const auto ts = Clock::now();
         for (Request *r : grp) r->t_start = ts;
-        int rc = run_group(S, grp);
+        int rc;
+        {
+            NvtxRange nvtx_("server decomposition group");
+            rc = run_group(S, grp);
+        }
         std::string msg = rc ? std::string(kc_last_error()) : std::string();
         {
             std::lock_guard<std::mutex> lk(S->mu);

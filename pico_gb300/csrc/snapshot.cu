@@ -164,6 +164,7 @@ extern "C" {
 
 int kc_graph_save(const kc_graph *g, const char *path) {
     clear_error();
+    NvtxRange nvtx_("kc_graph_save");
     if (!g || !path) return fail(KC_ERR_INVALID, "null argument");
     KC_CUDA(cudaSetDevice(g->device));
     KC_CUDA(cudaStreamSynchronize(g->stream));
@@ -199,6 +200,7 @@ int kc_graph_save(const kc_graph *g, const char *path) {
 
 int kc_graph_load(const char *path, int device, kc_graph **out) {
     clear_error();
+    NvtxRange nvtx_("kc_graph_load");
     if (!path || !out) return fail(KC_ERR_INVALID, "null argument");
     *out = nullptr;
     Mapping m;
@@ -237,6 +239,7 @@ int kc_graph_load(const char *path, int device, kc_graph **out) {
 
 int kc_graph_from_edge_file(const char *path, uint32_t flags, int device, kc_graph **out) {
     clear_error();
+    NvtxRange nvtx_("kc_graph_from_edge_file");
     if (!path || !out) return fail(KC_ERR_INVALID, "null argument");
     *out = nullptr;
     Mapping m;
@@ -276,6 +279,7 @@ int kc_graph_from_edge_file(const char *path, uint32_t flags, int device, kc_gra
 
 int kc_graph_kcore_subgraph(const kc_graph *g, uint32_t k, kc_graph **out, uint32_t *map_out, int map_on_device) {
     clear_error();
+    NvtxRange nvtx_("kc_graph_kcore_subgraph");
     if (!g || !out) return fail(KC_ERR_INVALID, "null argument");
     *out = nullptr;
     if (!g->core_valid) return fail(KC_ERR_STATE, "no decomposition has completed on this graph");
