@@ -12,7 +12,7 @@ Printed JSON line (rank 0):
              (CUDA events on the launching stream), inputs resident in HBM;
   e2e        the same metric through the C ABI with host buffers: each step
              copies the CSR host->device (pinned), decomposes, copies the core
-             array back and frees the graph; steps run from three host threads
+             array back and frees the graph; steps run from two host threads
              (independent graph handles), so one step's upload overlaps the
              previous step's decomposition (serial_value: one thread);
   roofline   algorithmic bytes B = 10*nnz + 16*n + 8 per decomposition over the
@@ -330,7 +330,7 @@ def run_engine(args, wl, world, rank, local, dist):
     core_view = np.ctypeslib.as_array((ctypes.c_uint32 * max(n, 1)).from_address(h_core.value))
     e2e_steps = max(4, min(args.steps, 12))
     mid = pg.method_id(method)
-    depth = 3
+    depth = 2
     h_cores = [h_core]
     for _ in range(depth - 1):
         extra = pg.ctypes.c_void_p()

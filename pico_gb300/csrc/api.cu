@@ -5,6 +5,8 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <thread>
+#include <vector>
 
 #include "kc_device.cuh"
 #include "kc_internal.h"
@@ -88,6 +90,63 @@ void dfree(void *p) {
     if (p) cudaFreeAsync(p, cudaStreamLegacy);
 }
 
+// Graph handles take their stream from a per-process pool and give it back
+// when freed: creating or destroying a stream can wait for a kernel that
+// another thread runs (a cooperative decomposition holds every SM), which
+// would serialise independent graphs built and freed while others decompose.
+static std::mutex g_stream_mu;
+static std::vector<std::pair<int, cudaStream_t>> g_stream_pool;
+
+cudaError_t acquire_stream(int device, cudaStream_t *s) {
+    {
+        std::lock_guard<std::mutex> lock(g_stream_mu);
+        for (size_t i = g_stream_pool.size(); i-- > 0;) {
+            if (g_stream_pool[i].first == device) {
+                *s = g_stream_pool[i].second;
+                g_stream_pool.erase(g_stream_pool.begin() + (std::ptrdiff_t)i);
+                return cudaSuccess;
+            }
+        }
+    }
+    return cudaStreamCreateWithFlags(s, cudaStreamNonBlocking);
+}
+
+void release_stream(int device, cudaStream_t s) {
+    std::lock_guard<std::mutex> lock(g_stream_mu);
+    if (g_stream_pool.size() < 256) g_stream_pool.emplace_back(device, s);
+    else cudaStreamDestroy(s);
+}
+
+// Events likewise: destroying one waits, like a stream, for another thread's
+// cooperative kernel.  Pooled events carry timing; they are handed back
+// after their last use has completed.
+static std::vector<std::pair<int, cudaEvent_t>> g_event_pool;
+
+cudaError_t acquire_event(cudaEvent_t *e) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    {
+        std::lock_guard<std::mutex> lock(g_stream_mu);
+        for (size_t i = g_event_pool.size(); i-- > 0;) {
+            if (g_event_pool[i].first == dev) {
+                *e = g_event_pool[i].second;
+                g_event_pool.erase(g_event_pool.begin() + (std::ptrdiff_t)i);
+                return cudaSuccess;
+            }
+        }
+    }
+    return cudaEventCreate(e);
+}
+
+void release_event(cudaEvent_t e) {
+    if (!e) return;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lock(g_stream_mu);
+    if (g_event_pool.size() < 1024) g_event_pool.emplace_back(dev, e);
+    else cudaEventDestroy(e);
+}
+
 Graph::~Graph() {
     int cur = 0;
     cudaGetDevice(&cur);
@@ -112,11 +171,11 @@ Graph::~Graph() {
     dfree(mcand);
     dfree(mvisit);
     dfree(mcount);
-    if (ev0) cudaEventDestroy(ev0);
-    if (ev1) cudaEventDestroy(ev1);
-    if (evk0) cudaEventDestroy(evk0);
-    if (evk1) cudaEventDestroy(evk1);
-    if (stream) cudaStreamDestroy(stream);
+    release_event(ev0);
+    release_event(ev1);
+    release_event(evk0);
+    release_event(evk1);
+    if (stream) release_stream(device, stream);  // idle: synchronised above
     cudaSetDevice(cur);
 }
 
@@ -138,8 +197,9 @@ static int new_graph(int device, kc_graph **out) {
     if (!g) return fail(KC_ERR_NOMEM, "host allocation of graph handle");
     g->device = device;
     cudaDeviceGetAttribute(&g->sm_count, cudaDevAttrMultiProcessorCount, device);
-    cudaError_t e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking);
+    cudaError_t e = acquire_stream(device, &g->stream);
     if (e != cudaSuccess) {
+        g->stream = nullptr;
         delete g;
         return fail(KC_ERR_CUDA, "stream create: %s", cudaGetErrorString(e));
     }
@@ -202,16 +262,16 @@ int kc_graph_from_edges_device(const uint32_t *d_src, const uint32_t *d_dst, uin
     kc_graph *g = nullptr;
     KC_TRY(new_graph(device, &g));
     cudaEvent_t a, b;
-    cudaEventCreate(&a);
-    cudaEventCreate(&b);
+    acquire_event(&a);
+    acquire_event(&b);
     cudaEventRecord(a, g->stream);
     int rc = build_csr_from_edges(g, d_src, d_dst, m, n, flags);
     cudaEventRecord(b, g->stream);
     cudaEventSynchronize(b);
     float ms = 0.f;
     cudaEventElapsedTime(&ms, a, b);
-    cudaEventDestroy(a);
-    cudaEventDestroy(b);
+    release_event(a);
+    release_event(b);
     if (rc) {
         delete g;
         return rc;
@@ -262,6 +322,33 @@ int kc_graph_from_mtx(const char *path, int mode, int device, kc_graph **out) {
     return rc;
 }
 
+// Largest degree and number of 32-wide virtual nodes of a CSR in host memory.
+static void host_degree_stats(const int64_t *rowptr, uint32_t n, uint32_t *maxdeg, uint64_t *vnodes) {
+    const unsigned nt = n < (1u << 16) ? 1u : std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    std::vector<uint32_t> mx(nt, 0);
+    std::vector<uint64_t> vn(nt, 0);
+    auto work = [&](unsigned t) {
+        const uint64_t lo = (uint64_t)n * t / nt, hi = (uint64_t)n * (t + 1) / nt;
+        uint32_t m = 0;
+        uint64_t c = 0;
+        for (uint64_t v = lo; v < hi; v++) {
+            const uint64_t d = (uint64_t)(rowptr[v + 1] - rowptr[v]);
+            m = std::max(m, (uint32_t)std::min<uint64_t>(d, 0xffffffffull));
+            c += (d + 31) / 32;
+        }
+        mx[t] = m;
+        vn[t] = c;
+    };
+    std::vector<std::thread> th;
+    for (unsigned t = 1; t < nt; t++) th.emplace_back(work, t);
+    work(0);
+    for (auto &x : th) x.join();
+    *maxdeg = *std::max_element(mx.begin(), mx.end());
+    uint64_t total = 0;
+    for (uint64_t x : vn) total += x;
+    *vnodes = total;
+}
+
 static int from_csr_common(const int64_t *rowptr, const uint32_t *col, uint32_t n, int device, kc_graph **out,
                            cudaMemcpyKind kind) {
     NvtxRange nvtx_("kc_graph_from_csr");
@@ -281,20 +368,26 @@ static int from_csr_common(const int64_t *rowptr, const uint32_t *col, uint32_t 
     if (!rc) rc = dalloc(&g->col, g->nnz + 1, "column ids");
     if (rc) { delete g; return rc; }
     cudaEvent_t a, b;
-    cudaEventCreate(&a);
-    cudaEventCreate(&b);
+    acquire_event(&a);
+    acquire_event(&b);
     cudaEventRecord(a, g->stream);
     cudaMemcpyAsync(g->rowptr, rowptr, ((uint64_t)n + 1) * 8, kind, g->stream);
     if (nnz) cudaMemcpyAsync(g->col, col, g->nnz * 4, kind, g->stream);
     cudaEventRecord(b, g->stream);
+    // a host CSR's statistics come from host threads while the copy runs, so
+    // building a graph needs no kernel (none has to wait for other work)
+    const bool host_stats = kind == cudaMemcpyHostToDevice;
+    if (host_stats) host_degree_stats(rowptr, n, &g->max_deg, &g->num_vnodes);
     e = cudaEventSynchronize(b);
     float ms = 0.f;
     cudaEventElapsedTime(&ms, a, b);
-    cudaEventDestroy(a);
-    cudaEventDestroy(b);
+    release_event(a);
+    release_event(b);
     if (e != cudaSuccess) { delete g; return fail(KC_ERR_CUDA, "CSR upload: %s", cudaGetErrorString(e)); }
-    rc = graph_finish(g);
-    if (rc) { delete g; return rc; }
+    if (!host_stats) {
+        rc = graph_finish(g);
+        if (rc) { delete g; return rc; }
+    }
     if (g->max_deg >= 0x7fffffffu) { delete g; return fail(KC_ERR_UNSUPPORTED, "degree above 2^31-1"); }
     g->build_ms = ms;
     *out = g;

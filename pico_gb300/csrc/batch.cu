@@ -541,12 +541,15 @@ kc_batch::~kc_batch() {
     kc::dfree(d_alist);
     kc::dfree(d_gtrace);
     for (int i = 0; i < 3; i++) {
-        if (side[i]) cudaStreamDestroy(side[i]);
-        if (join[i]) cudaEventDestroy(join[i]);
+        if (side[i]) {
+            cudaStreamSynchronize(side[i]);
+            kc::release_stream(g ? g->device : 0, side[i]);
+        }
+        kc::release_event(join[i]);
     }
-    if (fork) cudaEventDestroy(fork);
-    if (ev0) cudaEventDestroy(ev0);
-    if (ev1) cudaEventDestroy(ev1);
+    kc::release_event(fork);
+    kc::release_event(ev0);
+    kc::release_event(ev1);
     cudaSetDevice(cur);
 }
 
@@ -610,12 +613,12 @@ int kc_batch_create(kc_graph *g, const uint32_t *vbase, uint32_t num_graphs, kc_
     rc = dalloc(&b->d_F, b->F_cap, "batch row-chunk queue");
     if (!rc) {
         for (int i = 0; i < 3 && !rc; i++) {
-            if (cudaStreamCreateWithFlags(&b->side[i], cudaStreamNonBlocking) != cudaSuccess ||
-                cudaEventCreateWithFlags(&b->join[i], cudaEventDisableTiming) != cudaSuccess)
+            if (acquire_stream(g->device, &b->side[i]) != cudaSuccess ||
+                acquire_event(&b->join[i]) != cudaSuccess)
                 rc = fail(KC_ERR_CUDA, "batch streams");
         }
-        if (!rc && (cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess ||
-                    cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess))
+        if (!rc && (acquire_event(&b->fork) != cudaSuccess || acquire_event(&b->ev0) != cudaSuccess ||
+                    acquire_event(&b->ev1) != cudaSuccess))
             rc = fail(KC_ERR_CUDA, "batch events");
     }
     if (rc) {

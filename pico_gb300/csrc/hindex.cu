@@ -403,10 +403,10 @@ static int hindex_launch(Graph *g, cudaStream_t s, kc_stats *st, bool first_all)
 
 static int ensure_events(Graph *g) {
     if (!g->ev0) {
-        KC_CUDA(cudaEventCreate(&g->ev0));
-        KC_CUDA(cudaEventCreate(&g->ev1));
-        KC_CUDA(cudaEventCreate(&g->evk0));
-        KC_CUDA(cudaEventCreate(&g->evk1));
+        KC_CUDA(acquire_event(&g->ev0));
+        KC_CUDA(acquire_event(&g->ev1));
+        KC_CUDA(acquire_event(&g->evk0));
+        KC_CUDA(acquire_event(&g->evk1));
     }
     return KC_OK;
 }

@@ -28,6 +28,13 @@ struct NvtxRange {
 // Free device memory of the current device, including what this process's
 // allocator pool holds for reuse (api.cu).
 size_t device_free_bytes(size_t *total);
+// Non-blocking streams of `device` from a per-process pool (api.cu); a stream
+// is handed back idle.
+cudaError_t acquire_stream(int device, cudaStream_t *s);
+void release_stream(int device, cudaStream_t s);
+// Timing events of the current device from a per-process pool (api.cu).
+cudaError_t acquire_event(cudaEvent_t *e);
+void release_event(cudaEvent_t e);
 void clear_error();
 
 #define KC_CUDA(call)                                                                          \

@@ -847,10 +847,10 @@ int peel_run(Graph *g, cudaStream_t s, bool gpp_zero_to_one_flag, kc_stats *st) 
         g->gq_clean = true;
     }
     if (!g->ev0) {
-        KC_CUDA(cudaEventCreate(&g->ev0));
-        KC_CUDA(cudaEventCreate(&g->ev1));
-        KC_CUDA(cudaEventCreate(&g->evk0));
-        KC_CUDA(cudaEventCreate(&g->evk1));
+        KC_CUDA(acquire_event(&g->ev0));
+        KC_CUDA(acquire_event(&g->ev1));
+        KC_CUDA(acquire_event(&g->evk0));
+        KC_CUDA(acquire_event(&g->evk1));
     }
     PeelArgs A;
     A.rowptr = g->rowptr;
