@@ -1,0 +1,80 @@
+"""Independent graph handles used from several host threads at once (the
+end-to-end pipeline and the server do this): builds, decompositions of every
+method, updates and frees overlap, and every result stays exact."""
+from concurrent.futures import ThreadPoolExecutor
+
+import numpy as np
+import pytest
+
+import oracle
+import pico_gb300 as pg
+
+pytestmark = pytest.mark.gpu
+
+METHODS = ["peelone_dyn", "peel_dyn", "peelone", "gppeel", "histo", "cnt", "nbr"]
+
+
+def _case(i):
+    rng = np.random.default_rng(100 + i)
+    n = int(rng.integers(2000, 40000))
+    m = int(n * rng.uniform(2, 12))
+    s = rng.integers(0, n, m).astype(np.uint32)
+    d = rng.integers(0, n, m).astype(np.uint32)
+    rp, col = oracle.csr_dedup(n, s, d)
+    return rp, col, oracle.bz(rp, col)[0]
+
+
+def test_many_threads_build_decompose_free():
+    cases = [_case(i) for i in range(6)]
+
+    def work(i):
+        rp, col, ref = cases[i % len(cases)]
+        method = METHODS[i % len(METHODS)]
+        g = pg.Graph.from_csr(rp, col)
+        try:
+            core, _ = g.decompose(method)
+            want = np.where(np.diff(rp) == 0, 1, ref) if method == "gppeel" else ref
+            return bool(np.array_equal(core, want))
+        finally:
+            g.free()
+
+    with ThreadPoolExecutor(4) as ex:
+        results = list(ex.map(work, range(28)))
+    assert all(results)
+
+
+def test_updates_and_decompositions_in_parallel_threads():
+    big = pg.rmat_graph(16, 16, seed=3)
+    rp0, col0 = big.csr()
+    rng = np.random.default_rng(5)
+    n = big.n
+    src = np.repeat(np.arange(n, dtype=np.uint32), np.diff(rp0))
+    keep = src < col0
+    es, ed = src[keep], col0[keep]
+    pick = rng.choice(es.size, 600, replace=False)
+    dels = (es[pick], ed[pick])
+    ins = (rng.integers(0, n, 600).astype(np.uint32), rng.integers(0, n, 600).astype(np.uint32))
+    cases = [_case(i) for i in range(3)]
+
+    def upd(_):
+        big.set_param("update.incremental_max", 1 << 20)
+        big.update(ins, dels, want_core=False)
+        return True
+
+    def dec(i):
+        rp, col, ref = cases[i % 3]
+        g = pg.Graph.from_csr(rp, col)
+        try:
+            return bool(np.array_equal(g.decompose("peelone_dyn")[0], ref))
+        finally:
+            g.free()
+
+    with ThreadPoolExecutor(3) as ex:
+        fu = ex.submit(upd, 0)
+        results = list(ex.map(dec, range(9)))
+        assert fu.result()
+    assert all(results)
+    rp, col = big.csr()
+    core, _ = big.decompose("peelone_dyn")
+    assert np.array_equal(core, oracle.bz(rp, col)[0])
+    big.free()
