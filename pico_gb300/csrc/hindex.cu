@@ -92,20 +92,45 @@ __device__ __forceinline__ void hx_activate(const HxArgs &A, uint32_t u, unsigne
 
 // One warp: recompute vertex v (row length <= HX_WARP_MAX).  hist: this warp's
 // HX_WARP_MAX+1 shared bins.  Returns true if c[v] dropped.
+// Rows of at most HX_CACHE * 32 entries keep their neighbour ids and
+// estimates in registers: one gather pass serves the support test, the
+// histogram and the neighbour activation.
+constexpr int HX_CACHE = 4;
+
 __device__ bool hx_warp_vertex(const HxArgs &A, uint32_t v, unsigned nxt, uint32_t *hist, unsigned lane) {
     const int64_t s = A.rowptr[v], e = A.rowptr[v + 1];
     const uint32_t cap = __ldcg(&A.c[v]);
     if (cap == 0) return false;
+    const bool cached = e - s <= 32 * HX_CACHE;
+    uint32_t cu[HX_CACHE], cv[HX_CACHE];
     uint32_t cnt = 0;
-    for (int64_t j = s + lane; j < e; j += 32) cnt += __ldcg(&A.c[A.col[j]]) >= cap ? 1u : 0u;
+    if (cached) {
+#pragma unroll
+        for (int k = 0; k < HX_CACHE; k++) {
+            const int64_t j = s + k * 32 + lane;
+            cu[k] = j < e ? A.col[j] : 0xffffffffu;
+        }
+#pragma unroll
+        for (int k = 0; k < HX_CACHE; k++) cv[k] = cu[k] != 0xffffffffu ? __ldcg(&A.c[cu[k]]) : 0u;
+#pragma unroll
+        for (int k = 0; k < HX_CACHE; k++) cnt += (cu[k] != 0xffffffffu && cv[k] >= cap) ? 1u : 0u;
+    } else {
+        for (int64_t j = s + lane; j < e; j += 32) cnt += __ldcg(&A.c[A.col[j]]) >= cap ? 1u : 0u;
+    }
     cnt = __reduce_add_sync(KC_FULL_MASK, cnt);
     if (cnt >= cap) return false;  // support intact: estimate stands
     // histogram of min(c[u], cap) over bins [0, cap]; cap <= degree <= HX_WARP_MAX
     for (uint32_t b = lane; b <= cap; b += 32) hist[b] = 0;
     __syncwarp();
-    for (int64_t j = s + lane; j < e; j += 32) {
-        uint32_t x = __ldcg(&A.c[A.col[j]]);
-        atomicAdd(&hist[x < cap ? x : cap], 1u);
+    if (cached) {
+#pragma unroll
+        for (int k = 0; k < HX_CACHE; k++)
+            if (cu[k] != 0xffffffffu) atomicAdd(&hist[cv[k] < cap ? cv[k] : cap], 1u);
+    } else {
+        for (int64_t j = s + lane; j < e; j += 32) {
+            uint32_t x = __ldcg(&A.c[A.col[j]]);
+            atomicAdd(&hist[x < cap ? x : cap], 1u);
+        }
     }
     __syncwarp();
     // suffix scan from the top bin: largest k with sum_{x>=k} hist[x] >= k
@@ -131,10 +156,18 @@ __device__ bool hx_warp_vertex(const HxArgs &A, uint32_t v, unsigned nxt, uint32
     if (h >= cap) return false;
     if (lane == 0) A.c[v] = h;
     __syncwarp();
-    // neighbours whose estimate exceeds h may lose support
-    for (int64_t j = s + lane; j < e; j += 32) {
-        uint32_t u = A.col[j];
-        if (__ldcg(&A.c[u]) > h) hx_activate(A, u, nxt);
+    // neighbours whose estimate exceeds h may lose support (an estimate read
+    // earlier in this call is at least the current one, so it can only add
+    // activations)
+    if (cached) {
+#pragma unroll
+        for (int k = 0; k < HX_CACHE; k++)
+            if (cu[k] != 0xffffffffu && cv[k] > h) hx_activate(A, cu[k], nxt);
+    } else {
+        for (int64_t j = s + lane; j < e; j += 32) {
+            uint32_t u = A.col[j];
+            if (__ldcg(&A.c[u]) > h) hx_activate(A, u, nxt);
+        }
     }
     return true;
 }
