@@ -380,11 +380,19 @@ def run_engine(args, wl, world, rank, local, dist):
     for p in (h_rp, h_col, h_core):
         pg.lib().kc_host_free(p)
     g.free()
+    # the batched and serving sections are reported beside the headline; a
+    # failure there is recorded in its section instead of losing the line
     if world == 1 and not args.no_batch:
-        line["batched"] = batch_section(pg, device, sptr, args.steps, args.warmup, args.batch_graphs,
-                                        not args.no_autotune)
+        try:
+            line["batched"] = batch_section(pg, device, sptr, args.steps, args.warmup, args.batch_graphs,
+                                            not args.no_autotune)
+        except Exception as e:  # noqa: BLE001
+            line["batched"] = {"error": "%s: %s" % (type(e).__name__, e)}
     if world == 1 and not args.no_serve:
-        line["serving"] = serve_section(pg, device, args.serve_requests, args.serve_rate)
+        try:
+            line["serving"] = serve_section(pg, device, args.serve_requests, args.serve_rate)
+        except Exception as e:  # noqa: BLE001
+            line["serving"] = {"error": "%s: %s" % (type(e).__name__, e)}
     if rank == 0:
         print(json.dumps(line), flush=True)
     return 0
