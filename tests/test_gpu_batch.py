@@ -104,3 +104,37 @@ def test_large_graphs_in_global_memory(large_threads):
     assert np.array_equal(got, oracle.bz(rp, col)[0])
     b.free()
     g.free()
+
+
+def test_batch_size_classes_at_their_edges():
+    """Graphs that land in every size class: a star whose centre has degree
+    above 65,534 (uint32 degrees), a graph too large for shared memory (global
+    class), tiny graphs (1 and 2 vertices, an isolated vertex) and a clique;
+    the packed result equals Batagelj-Zaversnik graph by graph."""
+    parts = []
+    # star with 70,000 leaves: maxdeg above the uint16 range
+    leaves = np.arange(1, 70001, dtype=np.uint32)
+    parts.append((70001, np.zeros(leaves.size, np.uint32), leaves))
+    # 120,000-vertex random graph: above the shared-memory capacity
+    rng = np.random.default_rng(3)
+    parts.append((120000, rng.integers(0, 120000, 400000).astype(np.uint32),
+                  rng.integers(0, 120000, 400000).astype(np.uint32)))
+    parts.append((1, np.zeros(0, np.uint32), np.zeros(0, np.uint32)))  # one isolated vertex
+    parts.append((2, np.array([0], np.uint32), np.array([1], np.uint32)))
+    a, b = np.triu_indices(60, 1)
+    parts.append((60, a.astype(np.uint32), b.astype(np.uint32)))
+    vbase = [0]
+    src, dst = [], []
+    for n, s, d in parts:
+        src.append(s + vbase[-1])
+        dst.append(d + vbase[-1])
+        vbase.append(vbase[-1] + n)
+    src = np.concatenate(src)
+    dst = np.concatenate(dst)
+    g = pg.Graph.from_edges(src, dst, vbase[-1], dedup=True)
+    bt = pg.Batch(g, np.array(vbase, dtype=np.uint32))
+    got, _ = bt.decompose()
+    rp, col = g.csr()
+    assert np.array_equal(got, oracle.bz(rp, col)[0])
+    bt.free()
+    g.free()
