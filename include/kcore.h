@@ -209,7 +209,15 @@ int kc_graph_last_timing(const kc_graph *g, double *total_ms, double *kernel_ms)
 int kc_graph_set_param(kc_graph *g, const char *name, int64_t value);
 
 /* Per-level trace of the last peel decomposition (recorded when the "trace"
- * parameter is 1): one record per level index. */
+ * parameter is 1): one record per level index.  After an h-index
+ * decomposition (KC_HISTO / KC_CNT / KC_NBR) the records are per sweep:
+ * level = sweep index, claimed = estimates lowered, scan_len = vertices
+ * re-evaluated by one warp each, spilled = vertices re-evaluated by a whole
+ * CTA (rows above 512 entries), max_steal = the longest such row,
+ * t_work_end_ns = when the last CTA finished the sweep's vertices, cta_ns =
+ * CTA time on long rows, on short rows and in the sweep's barriers (the
+ * fourth is 0), steals = estimates lowered among the long rows; steal_fail
+ * and rounds are 0. */
 typedef struct kc_level_trace {
     uint64_t t_start_ns;  /* GPU global timer when the level began (CTA 0) */
     uint32_t level;       /* level value L */

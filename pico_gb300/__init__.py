@@ -408,7 +408,8 @@ class Graph:
         check(lib().kc_graph_set_param(self._h, name.encode(), int(value)))
 
     def trace(self):
-        """Per-level trace of the last peel (after set_param("trace", 1))."""
+        """Per-level trace of the last peel, or per-sweep trace of the last
+        h-index decomposition (after set_param("trace", 1))."""
         cnt = ctypes.c_uint32()
         check(lib().kc_graph_trace(self._h, None, 0, ctypes.byref(cnt)))
         buf = (kc_level_trace * max(cnt.value, 1))()

@@ -34,6 +34,7 @@ constexpr int HX_THREADS = 512;
 constexpr int HX_WARPS = HX_THREADS / 32;
 constexpr uint32_t HX_WARP_MAX = 512;   // rows up to this length: one warp
 constexpr uint32_t HX_BINS = 4096;      // CTA histogram bins
+constexpr unsigned HX_GRAB = 8;         // short-row vertices a warp takes per cursor step
 
 struct HxArgs {
     const int64_t *rowptr;
@@ -48,6 +49,8 @@ struct HxArgs {
     uint32_t max_sweeps;
     uint32_t first_all;  // sweep 0 covers every vertex (else list[0] / big[0])
     uint32_t withhold;   // CTA 0 never arrives at the first barrier (failure-detection hook)
+    PeelTrace *trace;    // per-sweep trace or nullptr
+    uint32_t trace_cap;
 };
 
 __global__ void hindex_init(const int64_t *__restrict__ rowptr, uint32_t n, uint32_t *c, uint32_t *inlist,
@@ -94,7 +97,8 @@ __device__ __forceinline__ void hx_activate(const HxArgs &A, uint32_t u, unsigne
 // HX_WARP_MAX+1 shared bins.  Returns true if c[v] dropped.
 // Rows of at most HX_CACHE * 32 entries keep their neighbour ids and
 // estimates in registers: one gather pass serves the support test, the
-// histogram and the neighbour activation.
+// histogram and the neighbour notification.  Longer rows run the support
+// test in chunks of HX_CACHE * 32 entries and stop once it holds.
 constexpr int HX_CACHE = 4;
 
 __device__ bool hx_warp_vertex(const HxArgs &A, uint32_t v, unsigned nxt, uint32_t *hist, unsigned lane) {
@@ -114,23 +118,40 @@ __device__ bool hx_warp_vertex(const HxArgs &A, uint32_t v, unsigned nxt, uint32
         for (int k = 0; k < HX_CACHE; k++) cv[k] = cu[k] != 0xffffffffu ? __ldcg(&A.c[cu[k]]) : 0u;
 #pragma unroll
         for (int k = 0; k < HX_CACHE; k++) cnt += (cu[k] != 0xffffffffu && cv[k] >= cap) ? 1u : 0u;
-    } else {
-        for (int64_t j = s + lane; j < e; j += 32) cnt += __ldcg(&A.c[A.col[j]]) >= cap ? 1u : 0u;
-    }
-    cnt = __reduce_add_sync(KC_FULL_MASK, cnt);
-    if (cnt >= cap) return false;  // support intact: estimate stands
-    // histogram of min(c[u], cap) over bins [0, cap]; cap <= degree <= HX_WARP_MAX
-    for (uint32_t b = lane; b <= cap; b += 32) hist[b] = 0;
-    __syncwarp();
-    if (cached) {
+        cnt = __reduce_add_sync(KC_FULL_MASK, cnt);
+        if (cnt >= cap) return false;  // support intact: estimate stands
+        // histogram of min(c[u], cap) over bins [0, cap]; cap <= degree <= HX_WARP_MAX
+        for (uint32_t b = lane; b <= cap; b += 32) hist[b] = 0;
+        __syncwarp();
 #pragma unroll
         for (int k = 0; k < HX_CACHE; k++)
             if (cu[k] != 0xffffffffu) atomicAdd(&hist[cv[k] < cap ? cv[k] : cap], 1u);
     } else {
-        for (int64_t j = s + lane; j < e; j += 32) {
-            uint32_t x = __ldcg(&A.c[A.col[j]]);
-            atomicAdd(&hist[x < cap ? x : cap], 1u);
+        // one pass builds the histogram of the values below cap and counts
+        // those at or above it (bin cap); it stops early once the support
+        // test holds
+        for (uint32_t b = lane; b < cap; b += 32) hist[b] = 0;
+        __syncwarp();
+        for (int64_t j0 = s; j0 < e && cnt < cap; j0 += 32 * HX_CACHE) {
+            uint32_t uu[HX_CACHE], c1 = 0;
+#pragma unroll
+            for (int k = 0; k < HX_CACHE; k++) {
+                const int64_t j = j0 + k * 32 + lane;
+                uu[k] = j < e ? A.col[j] : 0xffffffffu;
+            }
+            uint32_t xx[HX_CACHE];
+#pragma unroll
+            for (int k = 0; k < HX_CACHE; k++) xx[k] = uu[k] != 0xffffffffu ? __ldcg(&A.c[uu[k]]) : 0u;
+#pragma unroll
+            for (int k = 0; k < HX_CACHE; k++)
+                if (uu[k] != 0xffffffffu) {
+                    if (xx[k] >= cap) c1++;
+                    else atomicAdd(&hist[xx[k]], 1u);
+                }
+            cnt += __reduce_add_sync(KC_FULL_MASK, c1);
         }
+        if (cnt >= cap) return false;  // support intact: estimate stands
+        if (lane == 0) hist[cap] = cnt;
     }
     __syncwarp();
     // suffix scan from the top bin: largest k with sum_{x>=k} hist[x] >= k
@@ -156,19 +177,33 @@ __device__ bool hx_warp_vertex(const HxArgs &A, uint32_t v, unsigned nxt, uint32
     if (h >= cap) return false;
     if (lane == 0) A.c[v] = h;
     __syncwarp();
-    // neighbours whose estimate exceeds h may lose support (an estimate read
-    // earlier in this call is at least the current one, so it can only add
-    // activations)
+    // v stopped supporting exactly the neighbours u with h < c[u] <= cap.
+    // An estimate read earlier in this call is at least the current one; it
+    // can differ only if u was lowered concurrently in this sweep, and such a
+    // u re-examines itself in the next sweep (below), after this write.
     if (cached) {
 #pragma unroll
         for (int k = 0; k < HX_CACHE; k++)
-            if (cu[k] != 0xffffffffu && cv[k] > h) hx_activate(A, cu[k], nxt);
+            if (cu[k] != 0xffffffffu && cv[k] > h && cv[k] <= cap) hx_activate(A, cu[k], nxt);
     } else {
-        for (int64_t j = s + lane; j < e; j += 32) {
-            uint32_t u = A.col[j];
-            if (__ldcg(&A.c[u]) > h) hx_activate(A, u, nxt);
+        for (int64_t jb = s + lane; jb < e; jb += 32 * HX_CACHE) {
+            uint32_t uu[HX_CACHE], xx[HX_CACHE];
+#pragma unroll
+            for (int k = 0; k < HX_CACHE; k++) {
+                const int64_t j = jb + k * 32;
+                uu[k] = j < e ? A.col[j] : 0xffffffffu;
+            }
+#pragma unroll
+            for (int k = 0; k < HX_CACHE; k++) xx[k] = uu[k] != 0xffffffffu ? __ldcg(&A.c[uu[k]]) : 0u;
+#pragma unroll
+            for (int k = 0; k < HX_CACHE; k++)
+                if (uu[k] != 0xffffffffu && xx[k] > h && xx[k] <= cap) hx_activate(A, uu[k], nxt);
         }
     }
+    // A neighbour lowered in this sweep may have read c[v] before this write
+    // and skipped v (its window test saw the old, higher value) while this
+    // call counted it at its old estimate: v re-examines itself next sweep.
+    if (lane == 0) hx_activate(A, v, nxt);
     return true;
 }
 
@@ -245,43 +280,88 @@ __device__ bool hx_block_vertex(const HxArgs &A, uint32_t v, unsigned nxt, uint3
     __syncthreads();
     const uint32_t cap = cap_sh;
     if (cap == 0) return false;
-    uint32_t cnt = 0;
-    for (int64_t j = s + threadIdx.x; j < e; j += HX_THREADS) cnt += __ldcg(&A.c[A.col[j]]) >= cap ? 1u : 0u;
-    cnt = block_sum(cnt, red);
-    if (cnt >= cap) return false;
-    // narrow [lo, hi) -- known to contain h -- with 4096-bin passes until the
-    // bins are one value wide; `above` counts neighbours at >= hi
-    uint64_t lo = 0, hi = cap;
-    uint32_t h = 0;
-    for (;;) {
-        const uint64_t w = (hi - lo + HX_BINS - 1) / HX_BINS;
-        const int nb = (int)((hi - lo + w - 1) / w);
-        for (int b = threadIdx.x; b < (int)HX_BINS; b += HX_THREADS) hist[b] = 0;
+    // Support test in chunks that double from 2,048 entries; it stops as
+    // soon as cap neighbours at >= cap have been seen.  For cap <= HX_BINS
+    // the same pass builds the histogram of the values below cap.
+    const bool onepass = cap <= HX_BINS;
+    if (onepass) {
+        for (uint32_t b = threadIdx.x; b < cap; b += HX_THREADS) hist[b] = 0;
         __syncthreads();
-        uint32_t above = 0;
-        for (int64_t j = s + threadIdx.x; j < e; j += HX_THREADS) {
-            uint32_t x = __ldcg(&A.c[A.col[j]]);
-            if (x >= hi) above++;
-            else if (x >= lo) atomicAdd(&hist[(x - lo) / w], 1u);
+    }
+    uint32_t cnt = 0;
+    int64_t span = 4 * HX_THREADS;
+    for (int64_t j0 = s; j0 < e && cnt < cap; span *= 2) {
+        const int64_t j1 = e - j0 < span ? e : j0 + span;
+        uint32_t c1 = 0;
+        for (int64_t jb = j0 + threadIdx.x; jb < j1; jb += HX_CACHE * HX_THREADS) {
+            uint32_t uu[HX_CACHE], xx[HX_CACHE];
+#pragma unroll
+            for (int k = 0; k < HX_CACHE; k++) {
+                const int64_t j = jb + k * HX_THREADS;
+                uu[k] = j < j1 ? A.col[j] : 0xffffffffu;
+            }
+#pragma unroll
+            for (int k = 0; k < HX_CACHE; k++) xx[k] = uu[k] != 0xffffffffu ? __ldcg(&A.c[uu[k]]) : 0u;
+#pragma unroll
+            for (int k = 0; k < HX_CACHE; k++)
+                if (uu[k] != 0xffffffffu) {
+                    if (xx[k] >= cap) c1++;
+                    else if (onepass) atomicAdd(&hist[xx[k]], 1u);
+                }
         }
-        above = block_sum(above, red);
-        int b = hx_block_suffix_find(hist, nb, lo, w, above, red);
-        if (b < 0) b = 0;  // count(>= lo) >= lo holds by construction
-        if (w == 1) {
-            h = (uint32_t)(lo + b);
-            break;
+        cnt += block_sum(c1, red);
+        j0 = j1;
+    }
+    if (cnt >= cap) return false;
+    uint32_t h = 0;
+    if (onepass) {
+        const int b = hx_block_suffix_find(hist, (int)cap, 0, 1, cnt, red);
+        h = b < 0 ? 0u : (uint32_t)b;
+    } else {
+        // narrow [lo, hi) -- known to contain h -- with 4096-bin passes until
+        // the bins are one value wide; `above` counts neighbours at >= hi
+        uint64_t lo = 0, hi = cap;
+        for (;;) {
+            const uint64_t w = (hi - lo + HX_BINS - 1) / HX_BINS;
+            const int nb = (int)((hi - lo + w - 1) / w);
+            for (int b = threadIdx.x; b < (int)HX_BINS; b += HX_THREADS) hist[b] = 0;
+            __syncthreads();
+            uint32_t above = 0;
+            for (int64_t j = s + threadIdx.x; j < e; j += HX_THREADS) {
+                uint32_t x = __ldcg(&A.c[A.col[j]]);
+                if (x >= hi) above++;
+                else if (x >= lo) atomicAdd(&hist[(x - lo) / w], 1u);
+            }
+            above = block_sum(above, red);
+            int b = hx_block_suffix_find(hist, nb, lo, w, above, red);
+            if (b < 0) b = 0;  // count(>= lo) >= lo holds by construction
+            if (w == 1) {
+                h = (uint32_t)(lo + b);
+                break;
+            }
+            const uint64_t nlo = lo + (uint64_t)b * w;
+            hi = nlo + w < hi ? nlo + w : hi;
+            lo = nlo;
         }
-        const uint64_t nlo = lo + (uint64_t)b * w;
-        hi = nlo + w < hi ? nlo + w : hi;
-        lo = nlo;
     }
     if (h >= cap) return false;
     if (threadIdx.x == 0) A.c[v] = h;
     __syncthreads();
-    for (int64_t j = s + threadIdx.x; j < e; j += HX_THREADS) {
-        uint32_t u = A.col[j];
-        if (__ldcg(&A.c[u]) > h) hx_activate(A, u, nxt);
+    // notification window and self-requeue as in hx_warp_vertex
+    for (int64_t jb = s + threadIdx.x; jb < e; jb += HX_CACHE * HX_THREADS) {
+        uint32_t uu[HX_CACHE], xx[HX_CACHE];
+#pragma unroll
+        for (int k = 0; k < HX_CACHE; k++) {
+            const int64_t j = jb + k * HX_THREADS;
+            uu[k] = j < e ? A.col[j] : 0xffffffffu;
+        }
+#pragma unroll
+        for (int k = 0; k < HX_CACHE; k++) xx[k] = uu[k] != 0xffffffffu ? __ldcg(&A.c[uu[k]]) : 0u;
+#pragma unroll
+        for (int k = 0; k < HX_CACHE; k++)
+            if (uu[k] != 0xffffffffu && xx[k] > h && xx[k] <= cap) hx_activate(A, uu[k], nxt);
     }
+    if (threadIdx.x == 0) hx_activate(A, v, nxt);
     __syncthreads();
     return true;
 }
@@ -292,7 +372,7 @@ constexpr uint32_t HX_SMEM_WORDS =
 __global__ void __launch_bounds__(HX_THREADS, 2) hindex_kernel(HxArgs A) {
     __shared__ uint32_t hist[HX_SMEM_WORDS];
     __shared__ uint32_t red[HX_WARPS];
-    __shared__ unsigned int changed_sh;
+    __shared__ unsigned int changed_sh;  // estimates this CTA lowered in the sweep
     __shared__ unsigned long long item_sh;
     const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     HindexCtl *ctl = A.ctl;
@@ -316,8 +396,18 @@ __global__ void __launch_bounds__(HX_THREADS, 2) hindex_kernel(HxArgs A) {
         const unsigned cur = sweep & 1, nxt = cur ^ 1;
         if (threadIdx.x == 0) changed_sh = 0;
         __syncthreads();
-        // high-degree vertices: one CTA each, taken dynamically
+        const bool tr = A.trace != nullptr && sweep < A.trace_cap;
+        const unsigned long long t_sweep = tr ? global_ns() : 0ull;
         const unsigned long long nbig = ld_relaxed64(&ctl->big_len[cur]);
+        const bool all = sweep == 0 && A.first_all;
+        const unsigned long long nsmall = all ? (unsigned long long)A.n : ld_relaxed64(&ctl->list_len[cur]);
+        if (tr && blockIdx.x == 0 && threadIdx.x == 0) {
+            A.trace[sweep].t_start_ns = t_sweep;
+            A.trace[sweep].level = sweep;
+            A.trace[sweep].scan_len = (unsigned)nsmall;
+            A.trace[sweep].spilled = (unsigned)nbig;
+        }
+        // long rows: one CTA each, taken dynamically
         for (;;) {
             if (threadIdx.x == 0) item_sh = atomicAdd(&ctl->big_cursor, 1ull);
             __syncthreads();
@@ -325,30 +415,49 @@ __global__ void __launch_bounds__(HX_THREADS, 2) hindex_kernel(HxArgs A) {
             __syncthreads();
             if (i >= nbig) break;
             uint32_t v = A.big[cur][i];
-            if (!(sweep == 0 && A.first_all) && threadIdx.x == 0) atomicAnd(&A.inlist[v >> 5], ~(1u << (v & 31)));
+            if (!all && threadIdx.x == 0) atomicAnd(&A.inlist[v >> 5], ~(1u << (v & 31)));
             __syncthreads();
-            if (hx_block_vertex(A, v, nxt, hist, red) && threadIdx.x == 0) changed_sh = 1;
-            __syncthreads();
-        }
-        // the rest: one warp per vertex; sweep 0 covers every vertex
-        const bool all = sweep == 0 && A.first_all;
-        const unsigned long long nsmall = all ? (unsigned long long)A.n : ld_relaxed64(&ctl->list_len[cur]);
-        uint32_t *wh = hist + warp * (HX_WARP_MAX + 1);
-        bool wchanged = false;
-        for (unsigned long long i = (unsigned long long)blockIdx.x * HX_WARPS + warp; i < nsmall;
-             i += (unsigned long long)G * HX_WARPS) {
-            uint32_t v = all ? (uint32_t)i : A.list[cur][i];
-            if (all) {
-                if (A.rowptr[v + 1] - A.rowptr[v] > (int64_t)HX_WARP_MAX) continue;
-            } else if (lane == 0) {
-                atomicAnd(&A.inlist[v >> 5], ~(1u << (v & 31)));
+            const bool low = hx_block_vertex(A, v, nxt, hist, red);
+            if (low && threadIdx.x == 0) changed_sh++;
+            if (tr && threadIdx.x == 0) {
+                const int64_t len = A.rowptr[v + 1] - A.rowptr[v];
+                atomicMax(&A.trace[sweep].max_steal, len > 0xffffffffll ? 0xffffffffu : (unsigned)len);
+                if (low) atomicAdd(&A.trace[sweep].steals, 1u);
             }
-            __syncwarp();
-            wchanged |= hx_warp_vertex(A, v, nxt, wh, lane);
+            __syncthreads();
         }
-        if (lane == 0 && wchanged) changed_sh = 1;
+        const unsigned long long t_big = tr ? global_ns() : 0ull;
+        // short rows: one warp per vertex, HX_GRAB consecutive entries taken
+        // at a time from a shared cursor; sweep 0 covers every vertex
+        uint32_t *wh = hist + warp * (HX_WARP_MAX + 1);
+        unsigned wchanged = 0;
+        for (;;) {
+            unsigned long long base = 0;
+            if (lane == 0) base = atomicAdd(&ctl->cursor, (unsigned long long)HX_GRAB);
+            base = __shfl_sync(KC_FULL_MASK, base, 0);
+            if (base >= nsmall) break;
+            const unsigned long long end = nsmall - base < HX_GRAB ? nsmall : base + HX_GRAB;
+            for (unsigned long long i = base; i < end; i++) {
+                const uint32_t v = all ? (uint32_t)i : A.list[cur][i];
+                if (all) {
+                    if (A.rowptr[v + 1] - A.rowptr[v] > (int64_t)HX_WARP_MAX) continue;
+                } else if (lane == 0) {
+                    atomicAnd(&A.inlist[v >> 5], ~(1u << (v & 31)));
+                }
+                __syncwarp();
+                wchanged += hx_warp_vertex(A, v, nxt, wh, lane) ? 1u : 0u;
+            }
+        }
+        if (lane == 0 && wchanged) atomicAdd(&changed_sh, wchanged);
         __syncthreads();
         if (threadIdx.x == 0 && changed_sh) atomicOr(&ctl->changed, 1u);
+        const unsigned long long t_small = tr ? global_ns() : 0ull;
+        if (tr && threadIdx.x == 0) {
+            if (changed_sh) atomicAdd(&A.trace[sweep].claimed, changed_sh);
+            atomicAdd(&A.trace[sweep].cta_ns[0], t_big - t_sweep);
+            atomicAdd(&A.trace[sweep].cta_ns[1], t_small - t_big);
+            atomicMax(&A.trace[sweep].t_work_end_ns, t_small);
+        }
         if (!grid_barrier(&ctl->bar_count, &ctl->bar_gen, G, &ctl->err, KC_ERR_TIMEOUT, A.timeout_ns)) return;
         // one CTA resets the consumed lists; everyone reads the verdict after a second barrier
         __shared__ unsigned int go_on;
@@ -356,18 +465,20 @@ __global__ void __launch_bounds__(HX_THREADS, 2) hindex_kernel(HxArgs A) {
             ctl->list_len[cur] = 0;
             ctl->big_len[cur] = 0;
             ctl->big_cursor = 0;
+            ctl->cursor = 0;
             ctl->sweeps = sweep + 1;
             unsigned ch = ctl->changed;
             ctl->changed = 0;
             unsigned long long pend = ctl->list_len[nxt] + ctl->big_len[nxt];
-            ctl->cursor = (ch && pend > 0) ? 1ull : 0ull;  // reuse as the continue flag
+            ctl->go_on = (ch && pend > 0) ? 1u : 0u;
             if (sweep + 1 >= A.max_sweeps && pend > 0) atomicCAS(&ctl->err, 0u, (unsigned)KC_ERR_CAPACITY);
             __threadfence();
         }
         if (!grid_barrier(&ctl->bar_count, &ctl->bar_gen, G, &ctl->err, KC_ERR_TIMEOUT, A.timeout_ns)) return;
         // CTA 0 rewrites the flag only after the next sweep's first barrier,
         // by which time every CTA has read it
-        if (threadIdx.x == 0) go_on = (unsigned)ld_relaxed64(&ctl->cursor);
+        if (threadIdx.x == 0) go_on = ld_relaxed(&ctl->go_on);
+        if (tr && threadIdx.x == 0) atomicAdd(&A.trace[sweep].cta_ns[2], global_ns() - t_small);
         __syncthreads();
         if (!go_on) return;
     }
@@ -382,6 +493,14 @@ static int ensure_hx_buffers(Graph *g) {
         if (!g->big[i]) KC_TRY(dalloc(&g->big[i], n + 1, "active list (long rows)"));
     }
     if (!g->hctl) KC_TRY(dalloc(&g->hctl, 1, "h-index control"));
+    // one trace record per sweep; sweeps beyond the capacity are not recorded
+    const uint32_t tcap = (uint32_t)std::min<uint64_t>(n + 3, 65536);
+    if (g->tune.trace && (!g->trace || g->trace_cap < tcap)) {
+        dfree(g->trace);
+        g->trace = nullptr;
+        g->trace_cap = tcap;
+        KC_TRY(dalloc(&g->trace, g->trace_cap, "h-index trace"));
+    }
     return KC_OK;
 }
 
@@ -408,6 +527,9 @@ static int hindex_launch(Graph *g, cudaStream_t s, kc_stats *st, bool first_all)
     A.withhold = (unsigned)g->tune.withhold;
     A.max_sweeps = g->n + 3;  // a path needs O(n) sweeps
     A.first_all = first_all ? 1u : 0u;
+    A.trace = g->tune.trace ? g->trace : nullptr;
+    A.trace_cap = g->tune.trace ? g->trace_cap : 0;
+    if (A.trace) KC_CUDA(cudaMemsetAsync(g->trace, 0, sizeof(PeelTrace) * g->trace_cap, s));
     void *args[] = {&A};
     KC_CUDA(cudaEventRecord(g->evk0, s));
     KC_CUDA(cudaLaunchCooperativeKernel((const void *)hindex_kernel, dim3(grid), dim3(HX_THREADS), args, 0, s));
@@ -421,6 +543,7 @@ static int hindex_launch(Graph *g, cudaStream_t s, kc_stats *st, bool first_all)
     cudaEventElapsedTime(&kms, g->evk0, g->evk1);
     g->last_ms = ms;
     g->last_kernel_ms = kms;
+    g->trace_count = A.trace ? std::min<uint32_t>(h.sweeps, g->trace_cap) : 0;
     if (h.err) {
         g->core_valid = false;
         return fail((int)h.err, "h-index kernel raised error %u", h.err);

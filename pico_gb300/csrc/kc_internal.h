@@ -117,8 +117,9 @@ struct Tuning {
 struct HindexCtl {
     unsigned long long list_len[2];  // active list lengths (ping-pong)
     unsigned long long big_len[2];   // high-degree active list lengths
-    unsigned long long cursor;       // work cursor (small items)
+    unsigned long long cursor;       // work cursor (short-row items)
     unsigned long long big_cursor;   // work cursor (high-degree items)
+    unsigned int go_on;              // another sweep follows
     unsigned int bar_count;          // grid barrier arrivals
     unsigned int bar_gen;            // grid barrier generation
     unsigned int sweeps;
