@@ -164,6 +164,7 @@ Graph::~Graph() {
         dfree(big[i]);
     }
     dfree(hctl);
+    dfree(hx_bitmap);
     dfree(red);
     dfree(trace);
     dfree(mfront[0]);

@@ -11,11 +11,14 @@
 // support counters, neighbour flags), each as several launches plus a
 // blocking flag copy per iteration.  Here:
 //   * a vertex is re-examined only when a neighbour's estimate dropped from
-//     above its own (neighbour notification, deduplicated by a bitmap), so
-//     settled vertices read nothing;
-//   * the support test "at least c[v] neighbours at >= c[v]" runs first and
-//     settles most re-examined vertices without a histogram (the support
-//     counter of CntCore.cu:258-261 / the top bin of HistoCore.cu:184-198);
+//     at or above its own to below it (the neighbour stopped supporting it;
+//     notifications are deduplicated by one bitmap per sweep parity), or
+//     after its own estimate dropped, so settled vertices read nothing;
+//   * the support test "at least c[v] neighbours at >= c[v]" runs first,
+//     stops as soon as it holds and settles most re-examined vertices (the
+//     support counter of CntCore.cu:258-261 / the top bin of
+//     HistoCore.cu:184-198); when it fails, the same pass has built the
+//     histogram;
 //   * otherwise the h-index comes from a degree-capped histogram built in
 //     shared memory (one warp per vertex up to 512 neighbours; above that one
 //     CTA narrows the value range with 4096-bin passes until bins are one
@@ -41,7 +44,7 @@ struct HxArgs {
     const uint32_t *col;
     uint32_t n;
     uint32_t *c;
-    uint32_t *inlist;  // bitmap: vertex queued for the next sweep
+    uint32_t *inlist[2];  // bitmaps: vertex queued for the sweep of that parity
     uint32_t *list[2];
     uint32_t *big[2];
     HindexCtl *ctl;
@@ -53,8 +56,8 @@ struct HxArgs {
     uint32_t trace_cap;
 };
 
-__global__ void hindex_init(const int64_t *__restrict__ rowptr, uint32_t n, uint32_t *c, uint32_t *inlist,
-                            uint32_t *big0, HindexCtl *ctl) {
+__global__ void hindex_init(const int64_t *__restrict__ rowptr, uint32_t n, uint32_t *c, uint32_t *inlist0,
+                            uint32_t *inlist1, uint32_t *big0, HindexCtl *ctl) {
     const unsigned lane = threadIdx.x & 31;
     uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t base = blockIdx.x * (uint64_t)blockDim.x; base < n; base += stride) {
@@ -74,14 +77,20 @@ __global__ void hindex_init(const int64_t *__restrict__ rowptr, uint32_t n, uint
         }
     }
     uint64_t words = ((uint64_t)n + 31) / 32;
-    for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < words; w += stride) inlist[w] = 0u;
+    for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < words; w += stride) {
+        inlist0[w] = 0u;
+        inlist1[w] = 0u;
+    }
 }
 
-// Queue u for the next sweep unless it is queued already.
+// Queue u for the next sweep (list and bitmap of parity nxt) unless it is
+// queued already.  Vertices pending in the current sweep are queued again: a
+// notification never relies on an evaluation still to come in this sweep,
+// which could read the neighbour's estimate before its update is visible.
 __device__ __forceinline__ void hx_activate(const HxArgs &A, uint32_t u, unsigned nxt) {
     unsigned bit = 1u << (u & 31);
-    if (__ldcg(&A.inlist[u >> 5]) & bit) return;
-    unsigned old = atomicOr(&A.inlist[u >> 5], bit);
+    if (__ldcg(&A.inlist[nxt][u >> 5]) & bit) return;
+    unsigned old = atomicOr(&A.inlist[nxt][u >> 5], bit);
     if (old & bit) return;
     uint32_t d = (uint32_t)(A.rowptr[u + 1] - A.rowptr[u]);
     if (d > HX_WARP_MAX) {
@@ -101,8 +110,13 @@ __device__ __forceinline__ void hx_activate(const HxArgs &A, uint32_t u, unsigne
 // test in chunks of HX_CACHE * 32 entries and stop once it holds.
 constexpr int HX_CACHE = 4;
 
-__device__ bool hx_warp_vertex(const HxArgs &A, uint32_t v, unsigned nxt, uint32_t *hist, unsigned lane) {
+__device__ bool hx_warp_vertex(const HxArgs &A, uint32_t v, unsigned cur, bool clear, uint32_t *hist,
+                               unsigned lane) {
+    const unsigned nxt = cur ^ 1u;
     const int64_t s = A.rowptr[v], e = A.rowptr[v + 1];
+    // this sweep's bitmap is cleared as its vertices are examined, so it is
+    // empty when it becomes the next sweep's
+    if (clear && lane == 0) atomicAnd(&A.inlist[cur][v >> 5], ~(1u << (v & 31)));
     const uint32_t cap = __ldcg(&A.c[v]);
     if (cap == 0) return false;
     const bool cached = e - s <= 32 * HX_CACHE;
@@ -398,9 +412,9 @@ __global__ void __launch_bounds__(HX_THREADS, 2) hindex_kernel(HxArgs A) {
         __syncthreads();
         const bool tr = A.trace != nullptr && sweep < A.trace_cap;
         const unsigned long long t_sweep = tr ? global_ns() : 0ull;
-        const unsigned long long nbig = ld_relaxed64(&ctl->big_len[cur]);
         const bool all = sweep == 0 && A.first_all;
         const unsigned long long nsmall = all ? (unsigned long long)A.n : ld_relaxed64(&ctl->list_len[cur]);
+        const unsigned long long nbig = ld_relaxed64(&ctl->big_len[cur]);
         if (tr && blockIdx.x == 0 && threadIdx.x == 0) {
             A.trace[sweep].t_start_ns = t_sweep;
             A.trace[sweep].level = sweep;
@@ -415,7 +429,7 @@ __global__ void __launch_bounds__(HX_THREADS, 2) hindex_kernel(HxArgs A) {
             __syncthreads();
             if (i >= nbig) break;
             uint32_t v = A.big[cur][i];
-            if (!all && threadIdx.x == 0) atomicAnd(&A.inlist[v >> 5], ~(1u << (v & 31)));
+            if (!all && threadIdx.x == 0) atomicAnd(&A.inlist[cur][v >> 5], ~(1u << (v & 31)));
             __syncthreads();
             const bool low = hx_block_vertex(A, v, nxt, hist, red);
             if (low && threadIdx.x == 0) changed_sh++;
@@ -439,13 +453,8 @@ __global__ void __launch_bounds__(HX_THREADS, 2) hindex_kernel(HxArgs A) {
             const unsigned long long end = nsmall - base < HX_GRAB ? nsmall : base + HX_GRAB;
             for (unsigned long long i = base; i < end; i++) {
                 const uint32_t v = all ? (uint32_t)i : A.list[cur][i];
-                if (all) {
-                    if (A.rowptr[v + 1] - A.rowptr[v] > (int64_t)HX_WARP_MAX) continue;
-                } else if (lane == 0) {
-                    atomicAnd(&A.inlist[v >> 5], ~(1u << (v & 31)));
-                }
-                __syncwarp();
-                wchanged += hx_warp_vertex(A, v, nxt, wh, lane) ? 1u : 0u;
+                if (all && A.rowptr[v + 1] - A.rowptr[v] > (int64_t)HX_WARP_MAX) continue;
+                wchanged += hx_warp_vertex(A, v, cur, !all, wh, lane) ? 1u : 0u;
             }
         }
         if (lane == 0 && wchanged) atomicAdd(&changed_sh, wchanged);
@@ -467,10 +476,10 @@ __global__ void __launch_bounds__(HX_THREADS, 2) hindex_kernel(HxArgs A) {
             ctl->big_cursor = 0;
             ctl->cursor = 0;
             ctl->sweeps = sweep + 1;
-            unsigned ch = ctl->changed;
             ctl->changed = 0;
+            // a sweep that lowered nothing queued nothing
             unsigned long long pend = ctl->list_len[nxt] + ctl->big_len[nxt];
-            ctl->go_on = (ch && pend > 0) ? 1u : 0u;
+            ctl->go_on = pend > 0 ? 1u : 0u;
             if (sweep + 1 >= A.max_sweeps && pend > 0) atomicCAS(&ctl->err, 0u, (unsigned)KC_ERR_CAPACITY);
             __threadfence();
         }
@@ -488,6 +497,7 @@ static int ensure_hx_buffers(Graph *g) {
     const uint64_t n = g->n;
     if (!g->core) KC_TRY(dalloc(&g->core, n + 1, "core"));
     if (!g->bitmap) KC_TRY(dalloc(&g->bitmap, (n + 31) / 32 + 1, "active bitmap"));
+    if (!g->hx_bitmap) KC_TRY(dalloc(&g->hx_bitmap, (n + 31) / 32 + 1, "active bitmap (odd sweeps)"));
     for (int i = 0; i < 2; i++) {
         if (!g->list[i]) KC_TRY(dalloc(&g->list[i], n + 1, "active list"));
         if (!g->big[i]) KC_TRY(dalloc(&g->big[i], n + 1, "active list (long rows)"));
@@ -517,7 +527,8 @@ static int hindex_launch(Graph *g, cudaStream_t s, kc_stats *st, bool first_all)
     A.col = g->col;
     A.n = g->n;
     A.c = g->core;
-    A.inlist = g->bitmap;
+    A.inlist[0] = g->bitmap;
+    A.inlist[1] = g->hx_bitmap;
     A.list[0] = g->list[0];
     A.list[1] = g->list[1];
     A.big[0] = g->big[0];
@@ -525,7 +536,9 @@ static int hindex_launch(Graph *g, cudaStream_t s, kc_stats *st, bool first_all)
     A.ctl = g->hctl;
     A.timeout_ns = (unsigned long long)g->tune.wait_timeout_us * 1000ull;
     A.withhold = (unsigned)g->tune.withhold;
-    A.max_sweeps = g->n + 3;  // a path needs O(n) sweeps
+    // runaway guard only: every sweep but the one after a sweep without
+    // change lowers an estimate, so sweeps <= 2 * (nnz + 1)
+    A.max_sweeps = (uint32_t)std::min<uint64_t>(2 * ((uint64_t)g->nnz + 1) + 4, 0xffffffffull);
     A.first_all = first_all ? 1u : 0u;
     A.trace = g->tune.trace ? g->trace : nullptr;
     A.trace_cap = g->tune.trace ? g->trace_cap : 0;
@@ -573,7 +586,7 @@ int hindex_run(Graph *g, cudaStream_t s, kc_stats *st) {
     KC_CUDA(cudaEventRecord(g->ev0, s));
     KC_CUDA(cudaMemsetAsync(g->hctl, 0, sizeof(HindexCtl), s));
     const int ig = std::max(1, std::min<int>(g->sm_count * 8, (int)((g->n + 255) / 256)));
-    hindex_init<<<ig, 256, 0, s>>>(g->rowptr, g->n, g->core, g->bitmap, g->big[0], g->hctl);
+    hindex_init<<<ig, 256, 0, s>>>(g->rowptr, g->n, g->core, g->bitmap, g->hx_bitmap, g->big[0], g->hctl);
     return hindex_launch(g, s, st, true);
 }
 
@@ -599,6 +612,7 @@ int hindex_run_from(Graph *g, const uint32_t *d_list, uint64_t len, cudaStream_t
     KC_CUDA(cudaEventRecord(g->ev0, s));
     KC_CUDA(cudaMemsetAsync(g->hctl, 0, sizeof(HindexCtl), s));
     KC_CUDA(cudaMemsetAsync(g->bitmap, 0, ((uint64_t)g->n + 31) / 32 * 4, s));
+    KC_CUDA(cudaMemsetAsync(g->hx_bitmap, 0, ((uint64_t)g->n + 31) / 32 * 4, s));
     if (len) {
         const int ig = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)g->sm_count * 8, (len + 255) / 256));
         hindex_seed<<<ig, 256, 0, s>>>(g->rowptr, d_list, len, g->bitmap, g->list[0], g->big[0], g->hctl);

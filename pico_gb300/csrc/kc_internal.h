@@ -157,6 +157,7 @@ struct Graph {
     PeelCtl *peel_ctl = nullptr;
     uint32_t *list[2] = {nullptr, nullptr};  // h-index active lists
     uint32_t *big[2] = {nullptr, nullptr};   // h-index high-degree lists
+    uint32_t *hx_bitmap = nullptr;           // h-index pending bitmap of odd sweeps (even: bitmap)
     HindexCtl *hctl = nullptr;
     uint32_t *red = nullptr;          // small reduction scratch (min/max)
     // dynamic-graph maintenance

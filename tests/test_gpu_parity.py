@@ -208,6 +208,11 @@ def test_config2_rmat22_ef16():
         got, st = g.decompose(m)
         assert np.array_equal(got, core), m
         assert st.kmax == kmax
+    # the h-index sweeps race lowered estimates against pending-bit updates;
+    # repeated runs vary the interleaving
+    for _ in range(12):
+        got, _ = g.decompose("histo")
+        assert np.array_equal(got, core)
 
 
 def test_config3_rmat25_planted_core():
@@ -220,8 +225,9 @@ def test_config3_rmat25_planted_core():
     core, kmax = oracle.bz(rp, col)
     assert np.array_equal(got, core)
     assert st.kmax == kmax and kmax >= 2000  # the planted core dominates
-    got_h, _ = g.decompose("NbrCore")
-    assert np.array_equal(got_h, core)
+    for _ in range(6):
+        got_h, _ = g.decompose("NbrCore")
+        assert np.array_equal(got_h, core)
 
 
 def test_relabelling_and_local_core_property():
