@@ -348,7 +348,11 @@ __device__ bool hx_block_vertex(const HxArgs &A, uint32_t v, unsigned nxt, uint3
             }
             above = block_sum(above, red);
             int b = hx_block_suffix_find(hist, nb, lo, w, above, red);
-            if (b < 0) b = 0;  // count(>= lo) >= lo holds by construction
+            // The previous pass found count(>= lo) >= lo.  If estimates fell
+            // since, none of the bins qualifies: the h-index of the current
+            // estimates is below lo, so lo (bin 0) is still an upper bound of
+            // the core number, and v re-examines itself in the next sweep.
+            if (b < 0) b = 0;
             if (w == 1) {
                 h = (uint32_t)(lo + b);
                 break;
