@@ -73,3 +73,32 @@ def test_trace_records_levels():
     levels = [r["level"] for r in tr]
     assert levels == sorted(levels) and levels[0] == 0
     assert len({r["level"] for r in tr if r["claimed"]}) == st.levels == np.unique(core).size
+
+
+def test_trace_records_hindex_sweeps():
+    """After an h-index decomposition the trace holds one record per sweep:
+    sweep 0 examines every vertex (short rows by warps, rows above 512
+    entries by CTAs), the last sweep lowers nothing, and the estimates
+    lowered add up to at least the total drop from degree to core number in
+    steps of one vertex each."""
+    g = pg.rmat_graph(16, 16, seed=7)
+    rp, col = g.csr()
+    deg = np.diff(rp)
+    g.set_param("trace", 1)
+    core, st = g.decompose("histo")
+    want, _ = oracle.bz(rp, col)
+    assert np.array_equal(core, want)
+    tr = g.trace()
+    assert len(tr) == st.iterations >= 2
+    assert [r["level"] for r in tr] == list(range(len(tr)))
+    long_rows = int((deg > 512).sum())
+    assert tr[0]["spilled"] == long_rows and tr[0]["scan_len"] == g.n
+    assert tr[-1]["claimed"] == 0
+    lowered = sum(r["claimed"] for r in tr)
+    assert lowered >= int((core < deg).sum())
+    assert all(r["steals"] <= r["claimed"] for r in tr)
+    assert all(r["t_work_end_ns"] >= r["t_start_ns"] for r in tr)
+    g.set_param("trace", 0)
+    g.decompose("histo")
+    assert g.trace() == []
+    g.free()
