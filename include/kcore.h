@@ -198,7 +198,9 @@ int kc_graph_last_timing(const kc_graph *g, double *total_ms, double *kernel_ms)
  * "peel.threads" (threads per CTA, 512 or 256), "peel.balanced" (1 = each
  * processing round spreads at most "peel.round_entries" row entries evenly
  * over the CTA's threads), "peel.scan_unroll" (alive-list entries per
- * thread per scan tile, 4 or 8),
+ * thread per scan tile, 4 or 8), "hindex.warp_rows" (h-index: after the
+ * first sweep, rows up to this many entries are re-examined by one warp,
+ * longer ones by a whole CTA; default 8192),
  * "trace" (1 = record a per-level trace of the next decompositions),
  * "update.incremental_max" (largest update batch, in edges, maintained
  * incrementally by kc_graph_update), "wait.timeout_us" (limit of one

@@ -593,6 +593,9 @@ int kc_graph_set_param(kc_graph *g, const char *name, int64_t value) {
     } else if (k == "peel.scan_unroll") {
         if (value != 4 && value != 8) return fail(KC_ERR_INVALID, "peel.scan_unroll: 4 or 8");
         t.peel_scan_unroll = (int)value;
+    } else if (k == "hindex.warp_rows") {
+        if (value < 512 || value > (int64_t)1 << 30) return fail(KC_ERR_INVALID, "hindex.warp_rows: [512, 2^30]");
+        t.hindex_warp_rows = value;
     } else if (k == "trace") {
         t.trace = value ? 1 : 0;
     } else if (k == "update.incremental_max") {

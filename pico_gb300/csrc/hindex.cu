@@ -20,9 +20,11 @@
 //     HistoCore.cu:184-198); when it fails, the same pass has built the
 //     histogram;
 //   * otherwise the h-index comes from a degree-capped histogram built in
-//     shared memory (one warp per vertex up to 512 neighbours; above that one
-//     CTA narrows the value range with 4096-bin passes until bins are one
-//     value wide) and a warp-shuffle suffix scan;
+//     shared memory and a suffix scan: one warp per vertex whose row has at
+//     most 8,192 entries (512 in sweep 0, where estimates are still degrees),
+//     with a window of 512 values below the estimate; otherwise one CTA,
+//     which narrows the value range with 4096-bin passes until bins are one
+//     value wide;
 //   * updates are visible at once within a sweep (Gauss-Seidel), which only
 //     shortens the trajectory; sweeps are separated by a grid barrier with a
 //     bounded wait.
@@ -52,6 +54,7 @@ struct HxArgs {
     uint32_t max_sweeps;
     uint32_t first_all;  // sweep 0 covers every vertex (else list[0] / big[0])
     uint32_t withhold;   // CTA 0 never arrives at the first barrier (failure-detection hook)
+    uint32_t warp_rows;  // rows up to this length are re-examined by one warp
     PeelTrace *trace;    // per-sweep trace or nullptr
     uint32_t trace_cap;
 };
@@ -87,23 +90,79 @@ __global__ void hindex_init(const int64_t *__restrict__ rowptr, uint32_t n, uint
 // queued already.  Vertices pending in the current sweep are queued again: a
 // notification never relies on an evaluation still to come in this sweep,
 // which could read the neighbour's estimate before its update is visible.
+// Rows up to A.warp_rows entries (tunable "hindex.warp_rows") go to the warp list: one warp streams
+// such a row with fewer synchronisations than a CTA.  Rows above
+// HX_WARP_MAX entries are kept apart and handed out first, one per warp, so
+// that the short rows even out the end of the sweep.
 __device__ __forceinline__ void hx_activate(const HxArgs &A, uint32_t u, unsigned nxt) {
     unsigned bit = 1u << (u & 31);
     if (__ldcg(&A.inlist[nxt][u >> 5]) & bit) return;
     unsigned old = atomicOr(&A.inlist[nxt][u >> 5], bit);
     if (old & bit) return;
     uint32_t d = (uint32_t)(A.rowptr[u + 1] - A.rowptr[u]);
-    if (d > HX_WARP_MAX) {
+    if (d > A.warp_rows) {
         unsigned long long p = atomicAdd(&A.ctl->big_len[nxt], 1ull);
         A.big[nxt][p] = u;
+    } else if (d > HX_WARP_MAX) {
+        // medium rows fill the list from its far end (a vertex is listed
+        // once, so both ends together hold at most n entries)
+        unsigned long long p = atomicAdd(&A.ctl->mid_len[nxt], 1ull);
+        A.list[nxt][A.n - p] = u;
     } else {
         unsigned long long p = atomicAdd(&A.ctl->list_len[nxt], 1ull);
         A.list[nxt][p] = u;
     }
 }
 
-// One warp: recompute vertex v (row length <= HX_WARP_MAX).  hist: this warp's
-// HX_WARP_MAX+1 shared bins.  Returns true if c[v] dropped.
+// The largest k in [max(lo, 1), hi] with count(>= k) >= k, from the window
+// hist[k - lo] whose top bin hi - lo counts every value at or above hi; -1 if
+// none qualifies, and then carry = count(>= max(lo, 1)).
+__device__ __forceinline__ int64_t hx_warp_scan(const uint32_t *hist, uint32_t lo, uint32_t hi, unsigned lane,
+                                                uint32_t &carry) {
+    const int64_t kmin = lo > 1 ? (int64_t)lo : 1;
+    carry = 0;
+    for (int64_t top = (int64_t)hi; top >= kmin; top -= 32) {
+        const int64_t k = top - lane;
+        uint32_t incl = k >= kmin ? hist[k - lo] : 0u;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            uint32_t y = __shfl_up_sync(KC_FULL_MASK, incl, d);
+            if (lane >= (unsigned)d) incl += y;
+        }
+        const bool ok = k >= kmin && carry + incl >= (uint32_t)k;
+        const unsigned bb = __ballot_sync(KC_FULL_MASK, ok);
+        if (bb) return top - (__ffs(bb) - 1);
+        carry += __shfl_sync(KC_FULL_MASK, incl, 31);
+    }
+    return -1;
+}
+
+// The h-index lies below lo (above = count(>= lo)): windows of HX_WARP_MAX
+// values further down, each built from another pass over the row s..e.
+__device__ __forceinline__ uint32_t hx_warp_lower(const uint32_t *col, const uint32_t *c, int64_t s, int64_t e,
+                                               uint32_t *hist, uint32_t lo, uint32_t above, unsigned lane) {
+    for (;;) {
+        if (lo <= 1) return 0;  // no k >= 1 qualified
+        const uint32_t hi = lo;
+        lo = hi > HX_WARP_MAX ? hi - HX_WARP_MAX : 0u;
+        __syncwarp();
+        for (uint32_t b = lane; b < hi - lo; b += 32) hist[b] = 0;
+        if (lane == 0) hist[hi - lo] = above;
+        __syncwarp();
+        for (int64_t j = s + lane; j < e; j += 32) {
+            const uint32_t x = __ldcg(&c[col[j]]);
+            if (x < hi && x >= lo) atomicAdd(&hist[x - lo], 1u);
+        }
+        __syncwarp();
+        uint32_t carry;
+        const int64_t k = hx_warp_scan(hist, lo, hi, lane, carry);
+        if (k >= 0) return (uint32_t)k;
+        above = carry;
+    }
+}
+
+// One warp: recompute vertex v (any row length; long rows are streamed).
+// hist: this warp's HX_WARP_MAX+1 shared bins.  Returns true if c[v] dropped.
 // Rows of at most HX_CACHE * 32 entries keep their neighbour ids and
 // estimates in registers: one gather pass serves the support test, the
 // histogram and the neighbour notification.  Longer rows run the support
@@ -122,6 +181,7 @@ __device__ bool hx_warp_vertex(const HxArgs &A, uint32_t v, unsigned cur, bool c
     const bool cached = e - s <= 32 * HX_CACHE;
     uint32_t cu[HX_CACHE], cv[HX_CACHE];
     uint32_t cnt = 0;
+    uint32_t lo = 0;  // lowest value the histogram window covers
     if (cached) {
 #pragma unroll
         for (int k = 0; k < HX_CACHE; k++) {
@@ -134,17 +194,18 @@ __device__ bool hx_warp_vertex(const HxArgs &A, uint32_t v, unsigned cur, bool c
         for (int k = 0; k < HX_CACHE; k++) cnt += (cu[k] != 0xffffffffu && cv[k] >= cap) ? 1u : 0u;
         cnt = __reduce_add_sync(KC_FULL_MASK, cnt);
         if (cnt >= cap) return false;  // support intact: estimate stands
-        // histogram of min(c[u], cap) over bins [0, cap]; cap <= degree <= HX_WARP_MAX
+        // histogram of min(c[u], cap) over bins [0, cap]; cap <= degree <= 128
         for (uint32_t b = lane; b <= cap; b += 32) hist[b] = 0;
         __syncwarp();
 #pragma unroll
         for (int k = 0; k < HX_CACHE; k++)
             if (cu[k] != 0xffffffffu) atomicAdd(&hist[cv[k] < cap ? cv[k] : cap], 1u);
     } else {
-        // one pass builds the histogram of the values below cap and counts
-        // those at or above it (bin cap); it stops early once the support
-        // test holds
-        for (uint32_t b = lane; b < cap; b += 32) hist[b] = 0;
+        // One pass counts the values at or above cap and builds the histogram
+        // of those in the window [lo, cap) of at most HX_WARP_MAX values (bin
+        // x - lo); it stops early once the support test holds.
+        lo = cap > HX_WARP_MAX ? cap - HX_WARP_MAX : 0u;
+        for (uint32_t b = lane; b < cap - lo; b += 32) hist[b] = 0;
         __syncwarp();
         for (int64_t j0 = s; j0 < e && cnt < cap; j0 += 32 * HX_CACHE) {
             uint32_t uu[HX_CACHE], c1 = 0;
@@ -160,33 +221,20 @@ __device__ bool hx_warp_vertex(const HxArgs &A, uint32_t v, unsigned cur, bool c
             for (int k = 0; k < HX_CACHE; k++)
                 if (uu[k] != 0xffffffffu) {
                     if (xx[k] >= cap) c1++;
-                    else atomicAdd(&hist[xx[k]], 1u);
+                    else if (xx[k] >= lo) atomicAdd(&hist[xx[k] - lo], 1u);
                 }
             cnt += __reduce_add_sync(KC_FULL_MASK, c1);
         }
         if (cnt >= cap) return false;  // support intact: estimate stands
-        if (lane == 0) hist[cap] = cnt;
+        if (lane == 0) hist[cap - lo] = cnt;
     }
     __syncwarp();
-    // suffix scan from the top bin: largest k with sum_{x>=k} hist[x] >= k
-    uint32_t carry = 0, h = 0;
-    for (int64_t top = (int64_t)cap; top >= 1; top -= 32) {
-        int64_t k = top - lane;
-        uint32_t x = k >= 1 ? hist[k] : 0u;
-        uint32_t incl = x;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            uint32_t y = __shfl_up_sync(KC_FULL_MASK, incl, d);
-            if (lane >= (unsigned)d) incl += y;
-        }
-        bool ok = k >= 1 && carry + incl >= (uint32_t)k;
-        unsigned b = __ballot_sync(KC_FULL_MASK, ok);
-        if (b) {
-            h = (uint32_t)(top - (__ffs(b) - 1));
-            break;
-        }
-        carry += __shfl_sync(KC_FULL_MASK, incl, 31);
-    }
+    // Suffix scan of the window from its top bin: the largest k with
+    // count(>= k) >= k.  Estimates fall by little per sweep, so the h-index
+    // is nearly always in the first window.
+    uint32_t carry;
+    const int64_t hk = hx_warp_scan(hist, lo, cap, lane, carry);
+    const uint32_t h = hk >= 0 ? (uint32_t)hk : hx_warp_lower(A.col, A.c, s, e, hist, lo, carry, lane);
     __syncwarp();
     if (h >= cap) return false;
     if (lane == 0) A.c[v] = h;
@@ -418,11 +466,12 @@ __global__ void __launch_bounds__(HX_THREADS, 2) hindex_kernel(HxArgs A) {
         const unsigned long long t_sweep = tr ? global_ns() : 0ull;
         const bool all = sweep == 0 && A.first_all;
         const unsigned long long nsmall = all ? (unsigned long long)A.n : ld_relaxed64(&ctl->list_len[cur]);
+        const unsigned long long nmid = all ? 0ull : ld_relaxed64(&ctl->mid_len[cur]);
         const unsigned long long nbig = ld_relaxed64(&ctl->big_len[cur]);
         if (tr && blockIdx.x == 0 && threadIdx.x == 0) {
             A.trace[sweep].t_start_ns = t_sweep;
             A.trace[sweep].level = sweep;
-            A.trace[sweep].scan_len = (unsigned)nsmall;
+            A.trace[sweep].scan_len = (unsigned)(nsmall + nmid);
             A.trace[sweep].spilled = (unsigned)nbig;
         }
         // long rows: one CTA each, taken dynamically
@@ -445,10 +494,18 @@ __global__ void __launch_bounds__(HX_THREADS, 2) hindex_kernel(HxArgs A) {
             __syncthreads();
         }
         const unsigned long long t_big = tr ? global_ns() : 0ull;
-        // short rows: one warp per vertex, HX_GRAB consecutive entries taken
-        // at a time from a shared cursor; sweep 0 covers every vertex
+        // medium rows, one per warp, then short rows, HX_GRAB consecutive
+        // entries at a time, each taken from a shared cursor; sweep 0 covers
+        // every short row
         uint32_t *wh = hist + warp * (HX_WARP_MAX + 1);
         unsigned wchanged = 0;
+        while (nmid) {
+            unsigned long long i = 0;
+            if (lane == 0) i = atomicAdd(&ctl->mid_cursor, 1ull);
+            i = __shfl_sync(KC_FULL_MASK, i, 0);
+            if (i >= nmid) break;
+            wchanged += hx_warp_vertex(A, A.list[cur][A.n - i], cur, true, wh, lane) ? 1u : 0u;
+        }
         for (;;) {
             unsigned long long base = 0;
             if (lane == 0) base = atomicAdd(&ctl->cursor, (unsigned long long)HX_GRAB);
@@ -476,13 +533,15 @@ __global__ void __launch_bounds__(HX_THREADS, 2) hindex_kernel(HxArgs A) {
         __shared__ unsigned int go_on;
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             ctl->list_len[cur] = 0;
+            ctl->mid_len[cur] = 0;
             ctl->big_len[cur] = 0;
             ctl->big_cursor = 0;
+            ctl->mid_cursor = 0;
             ctl->cursor = 0;
             ctl->sweeps = sweep + 1;
             ctl->changed = 0;
             // a sweep that lowered nothing queued nothing
-            unsigned long long pend = ctl->list_len[nxt] + ctl->big_len[nxt];
+            unsigned long long pend = ctl->list_len[nxt] + ctl->mid_len[nxt] + ctl->big_len[nxt];
             ctl->go_on = pend > 0 ? 1u : 0u;
             if (sweep + 1 >= A.max_sweeps && pend > 0) atomicCAS(&ctl->err, 0u, (unsigned)KC_ERR_CAPACITY);
             __threadfence();
@@ -544,6 +603,7 @@ static int hindex_launch(Graph *g, cudaStream_t s, kc_stats *st, bool first_all)
     // change lowers an estimate, so sweeps <= 2 * (nnz + 1)
     A.max_sweeps = (uint32_t)std::min<uint64_t>(2 * ((uint64_t)g->nnz + 1) + 4, 0xffffffffull);
     A.first_all = first_all ? 1u : 0u;
+    A.warp_rows = (uint32_t)g->tune.hindex_warp_rows;
     A.trace = g->tune.trace ? g->trace : nullptr;
     A.trace_cap = g->tune.trace ? g->trace_cap : 0;
     if (A.trace) KC_CUDA(cudaMemsetAsync(g->trace, 0, sizeof(PeelTrace) * g->trace_cap, s));

@@ -108,6 +108,7 @@ struct Tuning {
     int peel_round_entries = 16384;
     int peel_scan_unroll = 4;  // alive-list entries per thread per scan tile: 4 or 8
     int trace = 0;
+    int64_t hindex_warp_rows = 8192;  // h-index: rows up to this length re-examined by one warp
     int64_t update_incremental_max = 512;  // larger update batches: full recompute (measured crossover ~1000 edges)
     int64_t wait_timeout_us = 2000000;       // limit of one inter-CTA wait
     int withhold = 0;  // failure-detection hook: one CTA never signals, so the others' waits run out
@@ -117,6 +118,8 @@ struct Tuning {
 struct HindexCtl {
     unsigned long long list_len[2];  // active list lengths (ping-pong)
     unsigned long long big_len[2];   // high-degree active list lengths
+    unsigned long long mid_len[2];   // medium rows, stored from the far end of list[]
+    unsigned long long mid_cursor;   // work cursor (medium rows)
     unsigned long long cursor;       // work cursor (short-row items)
     unsigned long long big_cursor;   // work cursor (high-degree items)
     unsigned int go_on;              // another sweep follows

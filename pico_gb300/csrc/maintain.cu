@@ -46,9 +46,6 @@ __device__ __forceinline__ uint32_t lower_bound_u32(const uint32_t *a, uint32_t 
     return lo;
 }
 
-// Phase 1, one warp per row with changes: the positions (in the old row) of
-// entries to delete and the values to insert, each sorted, and the new row
-// length.  A pair both deleted and inserted stays as it is.
 // Every row: new length = old length, no changes yet; flags the rows that
 // the change lists touch.
 __global__ void mark_changed(const int64_t *__restrict__ rowptr, uint32_t n, const int64_t *__restrict__ drp,
