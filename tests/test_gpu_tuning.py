@@ -102,3 +102,36 @@ def test_trace_records_hindex_sweeps():
     g.decompose("histo")
     assert g.trace() == []
     g.free()
+
+
+@pytest.mark.parametrize("warp_rows", [512, 2048, 1 << 30])
+def test_hindex_warp_rows(warp_rows):
+    """Rows above 512 entries re-examined by one warp (windowed histogram
+    below the estimate) or by a whole CTA: the same core numbers as
+    Batagelj-Zaversnik, on R-MAT graphs with hubs and on a graph whose hub
+    loses most of its support (a 700-clique whose vertices also hold long
+    pendant stars, joined to a 1,500-leaf hub)."""
+    g = pg.rmat_graph(16, 16, seed=11)
+    rp, col = g.csr()
+    want, _ = oracle.bz(rp, col)
+    g.set_param("hindex.warp_rows", warp_rows)
+    for method in ("histo", "cnt", "nbr"):
+        got, _ = g.decompose(method)
+        assert np.array_equal(got, want), method
+    g.free()
+    a, b = np.triu_indices(700, 1)
+    src = [a, np.zeros(1500, np.int64)]
+    dst = [b, 700 + np.arange(1500)]
+    src.append(np.zeros(600, np.int64))  # the hub also touches the clique
+    dst.append(np.arange(1, 601))
+    n = 2200 + 700 * 20
+    src.append(np.repeat(np.arange(700), 20))  # 20 leaves per clique vertex
+    dst.append(2200 + np.arange(700 * 20))
+    h = pg.Graph.from_edges(np.concatenate(src).astype(np.uint32), np.concatenate(dst).astype(np.uint32), n,
+                            dedup=True)
+    h.set_param("hindex.warp_rows", warp_rows)
+    rp, col = h.csr()
+    want, _ = oracle.bz(rp, col)
+    got, _ = h.decompose("histo")
+    assert np.array_equal(got, want)
+    h.free()
