@@ -19,7 +19,11 @@ Printed JSON line (rank 0):
              main kernel's average CUDA-event duration, against the measured
              HBM copy bandwidth;
   cpu_baseline  serial Batagelj-Zaversnik (the oracle) on the same graph, on
-             one host core.
+             one host core;
+  batched / serving / inputs  the 4096-graph batched form against the plain
+             form, the request server's latency, and the input/output paths
+             (generation, edge files, MatrixMarket parse, snapshots, k-core
+             extraction).
 `--impl reference` times the reference's CPU path (serial Batagelj-Zaversnik,
 the oracle port) on the host cores on the same graph, generated on the host.
 `--gpus N` (under torchrun) runs N independent replicas: the decomposition of
@@ -393,9 +397,105 @@ def run_engine(args, wl, world, rank, local, dist):
             line["serving"] = serve_section(pg, device, args.serve_requests, args.serve_rate)
         except Exception as e:  # noqa: BLE001
             line["serving"] = {"error": "%s: %s" % (type(e).__name__, e)}
+    if world == 1 and not args.no_inputs:
+        try:
+            line["inputs"] = inputs_section(pg, device, wl, rowptr, col, st.kmax)
+        except Exception as e:  # noqa: BLE001
+            line["inputs"] = {"error": "%s: %s" % (type(e).__name__, e)}
     if rank == 0:
         print(json.dumps(line), flush=True)
     return 0
+
+
+def inputs_section(pg, device, wl, rowptr, col, kmax):
+    """The input and output paths around the decomposition, timed on the host
+    clock (each call returns with its result on the device or host): device
+    generation and CSR build of the workload graph, a binary edge file
+    (mmap, upload, de-duplicating device build), a MatrixMarket text parse on
+    a smaller R-MAT graph, snapshot save and load, a device build from host
+    edge arrays, and induced k-core extraction.  Files are written first and
+    read back while page-cached, so these are parse / upload / build rates,
+    not disk rates."""
+    import tempfile
+
+    import numpy as np
+    import torch
+
+    out = {"workload": wl["desc"].split(";")[0]}
+
+    def clock(fn):
+        torch.cuda.synchronize(device)
+        t0 = time.perf_counter()
+        r = fn()
+        torch.cuda.synchronize(device)
+        return r, 1e3 * (time.perf_counter() - t0)
+
+    if wl["kind"] == "rmat":
+        g, ms = clock(lambda: pg.rmat_graph(wl["scale"], wl["ef"], wl["seed"], device=device))
+        out["generate_and_build_ms"] = round(ms, 2)
+        g.free()
+    n = rowptr.size - 1
+    src = np.repeat(np.arange(n, dtype=np.uint32), np.diff(rowptr))
+    up = src < col  # each undirected edge once
+    us, ud = src[up], col[up]
+    m = int(us.size)
+    with tempfile.TemporaryDirectory() as tmp:
+        # binary edge file: little-endian uint32 (src, dst) pairs
+        path = os.path.join(tmp, "edges.bin")
+        np.stack([us, ud], axis=1).astype("<u4").tofile(path)
+        nbytes = os.path.getsize(path)
+        g, ms = clock(lambda: pg.Graph.from_edge_file(path, dedup=True, device=device))
+        assert g.nnz == col.size
+        out["edge_file"] = {"bytes": nbytes, "edges": m, "ms": round(ms, 2),
+                            "GB_per_s": round(nbytes / ms / 1e6, 2)}
+        g.free()
+        os.remove(path)
+        # host edge arrays -> device CSR with de-duplication
+        g, ms = clock(lambda: pg.Graph.from_edges(us, ud, n, dedup=True, device=device))
+        assert g.nnz == col.size
+        out["from_host_edges_ms"] = round(ms, 2)
+        # snapshot of the decomposed graph
+        g.decompose_device("peelone_dyn")
+        path = os.path.join(tmp, "graph.kcsnap")
+        _, ms_save = clock(lambda: g.save(path))
+        nbytes = os.path.getsize(path)
+        h, ms_load = clock(lambda: pg.Graph.load(path, device=device))
+        assert h.nnz == g.nnz
+        h.free()
+        os.remove(path)
+        out["snapshot"] = {"bytes": nbytes, "save_ms": round(ms_save, 2), "load_ms": round(ms_load, 2),
+                           "save_GB_per_s": round(nbytes / ms_save / 1e6, 2),
+                           "load_GB_per_s": round(nbytes / ms_load / 1e6, 2)}
+        # induced k-core of the decomposition
+        k = max(1, kmax // 2)
+        (sub, ids), ms = clock(lambda: g.kcore_subgraph(k))
+        out["kcore_subgraph"] = {"k": k, "ms": round(ms, 2), "n_out": sub.n, "nnz_out": sub.nnz}
+        sub.free()
+        g.free()
+        # MatrixMarket text (the reference's input format) of R-MAT scale 17
+        g2 = pg.rmat_graph(17, 16, 9, device=device)
+        rp2, col2 = g2.csr()
+        g2.free()
+        s2 = np.repeat(np.arange(rp2.size - 1, dtype=np.uint32), np.diff(rp2))
+        up2 = s2 < col2
+        e2 = np.stack([s2[up2] + 1, col2[up2] + 1], axis=1)
+        path = os.path.join(tmp, "rmat17.mtx")
+        with open(path, "w") as f:
+            f.write("%%%%MatrixMarket matrix coordinate pattern symmetric\n%d %d %d\n"
+                    % (rp2.size - 1, rp2.size - 1, e2.shape[0]))
+            f.write("\n".join("%d %d" % (a, b) for a, b in e2.tolist()))
+            f.write("\n")
+        nbytes = os.path.getsize(path)
+        (_, ps, _), ms_parse = clock(lambda: pg.parse_mtx(path, mode="coo"))
+        assert ps.size == e2.shape[0]
+        g3, ms_csr = clock(lambda: pg.Graph.from_mtx(path, mode="csr", device=device))
+        assert g3.nnz == col2.size
+        g3.free()
+        out["mtx_text"] = {"graph": "R-MAT scale 17, edge factor 16, seed 9", "bytes": nbytes,
+                           "edges": int(e2.shape[0]), "parse_ms": round(ms_parse, 2),
+                           "parse_MB_per_s": round(nbytes / ms_parse / 1e3, 1),
+                           "to_device_csr_ms": round(ms_csr, 2), "host_threads": os.cpu_count()}
+    return out
 
 
 BATCH_DESC = ("4096 graphs, n = floor(10^U(2,5)), generator uniform over Erdos-Renyi / R-MAT (a,b,c=.57,.19,.19) / "
@@ -523,6 +623,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-batch", action="store_true", help="skip the 4096-graph batched-vs-plain section")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving section")
+    ap.add_argument("--no-inputs", action="store_true", help="skip the input/output path section")
     ap.add_argument("--batch-graphs", type=int, default=4096, help="graphs in the batched section")
     ap.add_argument("--no-autotune", action="store_true", help="batched section: keep the default configuration")
     ap.add_argument("--serve-requests", type=int, default=40)
