@@ -269,6 +269,91 @@ __device__ bool hx_warp_vertex(const HxArgs &A, uint32_t v, unsigned cur, bool c
     return true;
 }
 
+// Four vertices per warp, one per group of 8 lanes, for rows of at most
+// HX_TINY entries (4 per lane): the same steps as hx_warp_vertex (pending
+// bit, support test, histogram of min(c[u], cap) over [0, cap] in the
+// group's HX_TINY + 1 bins, suffix scan, notification window, self-requeue)
+// with group-wide shuffles.  vg / valid: the vertex of this lane's group.
+// Returns the number of estimates lowered (the same on every lane).
+constexpr uint32_t HX_TINY = 32;
+
+__device__ unsigned hx_warp_tiny(const HxArgs &A, uint32_t vg, bool valid, unsigned cur, bool clear,
+                                 uint32_t *hist, unsigned lane) {
+    const unsigned nxt = cur ^ 1u;
+    const unsigned gi = lane >> 3, gl = lane & 7;
+    int64_t s = 0, e = 0;
+    uint32_t cap = 0;
+    if (valid) {
+        s = A.rowptr[vg];
+        e = A.rowptr[vg + 1];
+        if (clear && gl == 0) atomicAnd(&A.inlist[cur][vg >> 5], ~(1u << (vg & 31)));
+        cap = __ldcg(&A.c[vg]);
+    }
+    uint32_t cu[4], cv[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const int64_t j = s + gl + 8 * k;
+        cu[k] = valid && j < e ? A.col[j] : 0xffffffffu;
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++) cv[k] = cu[k] != 0xffffffffu ? __ldcg(&A.c[cu[k]]) : 0u;
+    uint32_t cnt = 0;
+#pragma unroll
+    for (int k = 0; k < 4; k++) cnt += (cu[k] != 0xffffffffu && cv[k] >= cap) ? 1u : 0u;
+    cnt += __shfl_xor_sync(KC_FULL_MASK, cnt, 1);
+    cnt += __shfl_xor_sync(KC_FULL_MASK, cnt, 2);
+    cnt += __shfl_xor_sync(KC_FULL_MASK, cnt, 4);
+    const bool act = valid && cap > 0 && cnt < cap;  // the same on the group's lanes
+    uint32_t *hb = hist + gi * (HX_TINY + 1);
+    if (act)
+        for (uint32_t b = gl; b <= cap; b += 8) hb[b] = 0;
+    __syncwarp();
+    if (act) {
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            if (cu[k] != 0xffffffffu) atomicAdd(&hb[cv[k] < cap ? cv[k] : cap], 1u);
+    }
+    __syncwarp();
+    // lane gl holds bins cap - 4 gl - t (t = 0..3, from the top): suffix
+    // counts from the bins of the lanes before it, then its own
+    uint32_t loc[4], lsum = 0;
+#pragma unroll
+    for (int t = 0; t < 4; t++) {
+        const int k = (int)cap - 4 * (int)gl - t;
+        loc[t] = act && k >= 1 ? hb[k] : 0u;
+        lsum += loc[t];
+    }
+    uint32_t run = lsum;
+#pragma unroll
+    for (int d = 1; d < 8; d <<= 1) {
+        const uint32_t y = __shfl_up_sync(KC_FULL_MASK, run, d, 8);
+        if (gl >= (unsigned)d) run += y;
+    }
+    run -= lsum;
+    int best = 0;  // the largest k with count(>= k) >= k (0 if none)
+#pragma unroll
+    for (int t = 0; t < 4; t++) {
+        const int k = (int)cap - 4 * (int)gl - t;
+        run += loc[t];
+        if (act && k >= 1 && run >= (uint32_t)k && best == 0) best = k;
+    }
+    best = max(best, __shfl_xor_sync(KC_FULL_MASK, best, 1));
+    best = max(best, __shfl_xor_sync(KC_FULL_MASK, best, 2));
+    best = max(best, __shfl_xor_sync(KC_FULL_MASK, best, 4));
+    const uint32_t h = (uint32_t)best;
+    const bool low = act && h < cap;
+    if (low && gl == 0) A.c[vg] = h;
+    __syncwarp();
+    if (low) {
+        // notification window and self-requeue as in hx_warp_vertex
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            if (cu[k] != 0xffffffffu && cv[k] > h && cv[k] <= cap) hx_activate(A, cu[k], nxt);
+        if (gl == 0) hx_activate(A, vg, nxt);
+    }
+    return (unsigned)__popc(__ballot_sync(KC_FULL_MASK, low && gl == 0));
+}
+
 // Block-wide helpers for the CTA path.
 __device__ __forceinline__ uint32_t block_sum(uint32_t x, uint32_t *red) {
     x = __reduce_add_sync(KC_FULL_MASK, x);
@@ -511,10 +596,34 @@ __global__ void __launch_bounds__(HX_THREADS, 2) hindex_kernel(HxArgs A) {
             if (lane == 0) base = atomicAdd(&ctl->cursor, (unsigned long long)HX_GRAB);
             base = __shfl_sync(KC_FULL_MASK, base, 0);
             if (base >= nsmall) break;
-            const unsigned long long end = nsmall - base < HX_GRAB ? nsmall : base + HX_GRAB;
-            for (unsigned long long i = base; i < end; i++) {
-                const uint32_t v = all ? (uint32_t)i : A.list[cur][i];
-                if (all && A.rowptr[v + 1] - A.rowptr[v] > (int64_t)HX_WARP_MAX) continue;
+            const unsigned cntv = (unsigned)(nsmall - base < HX_GRAB ? nsmall - base : HX_GRAB);
+            // the grab's vertices and row lengths on lanes 0..cntv-1; rows
+            // of at most HX_TINY entries go four at a time, the others one
+            // per warp (sweep 0 leaves rows above HX_WARP_MAX to the CTAs)
+            uint32_t vi = 0;
+            int64_t di = 0;
+            if (lane < cntv) {
+                vi = all ? (uint32_t)(base + lane) : A.list[cur][base + lane];
+                di = A.rowptr[vi + 1] - A.rowptr[vi];
+            }
+            const bool in = lane < cntv && !(all && di > (int64_t)HX_WARP_MAX);
+            unsigned tinym = __ballot_sync(KC_FULL_MASK, in && di <= (int64_t)HX_TINY);
+            unsigned restm = __ballot_sync(KC_FULL_MASK, in && di > (int64_t)HX_TINY);
+            while (tinym) {
+                int pick = -1;  // this lane's group takes the (lane / 8)-th remaining tiny vertex
+#pragma unroll
+                for (unsigned g2 = 0; g2 < 4; g2++) {
+                    const int p = tinym ? __ffs(tinym) - 1 : -1;
+                    if (g2 == (lane >> 3)) pick = p;
+                    tinym &= tinym - 1u;
+                }
+                const uint32_t vg = __shfl_sync(KC_FULL_MASK, vi, pick < 0 ? 0 : pick);
+                wchanged += hx_warp_tiny(A, vg, pick >= 0, cur, !all, wh, lane);
+            }
+            while (restm) {
+                const int p = __ffs(restm) - 1;
+                restm &= restm - 1u;
+                const uint32_t v = __shfl_sync(KC_FULL_MASK, vi, p);
                 wchanged += hx_warp_vertex(A, v, cur, !all, wh, lane) ? 1u : 0u;
             }
         }
