@@ -20,9 +20,10 @@
 //     HistoCore.cu:184-198); when it fails, the same pass has built the
 //     histogram;
 //   * otherwise the h-index comes from a degree-capped histogram built in
-//     shared memory and a suffix scan: one warp per vertex whose row has at
-//     most 8,192 entries (512 in sweep 0, where estimates are still degrees),
-//     with a window of 512 values below the estimate; otherwise one CTA,
+//     shared memory and a suffix scan: 8 lanes per vertex for rows of at
+//     most 32 entries, one warp per vertex for rows of at most 8,192 entries
+//     (512 in sweep 0, where estimates are still degrees), with a window of
+//     512 values below the estimate; otherwise one CTA,
 //     which narrows the value range with 4096-bin passes until bins are one
 //     value wide;
 //   * updates are visible at once within a sweep (Gauss-Seidel), which only
