@@ -169,6 +169,7 @@ __device__ __forceinline__ uint32_t hx_warp_lower(const uint32_t *col, const uin
 // histogram and the neighbour notification.  Longer rows run the support
 // test in chunks of HX_CACHE * 32 entries and stop once it holds.
 constexpr int HX_CACHE = 4;
+constexpr int HX_STREAM = 4;  // row entries in flight per lane when a warp streams a long row (8: slower, spills)
 
 __device__ bool hx_warp_vertex(const HxArgs &A, uint32_t v, unsigned cur, bool clear, uint32_t *hist,
                                unsigned lane) {
@@ -208,18 +209,18 @@ __device__ bool hx_warp_vertex(const HxArgs &A, uint32_t v, unsigned cur, bool c
         lo = cap > HX_WARP_MAX ? cap - HX_WARP_MAX : 0u;
         for (uint32_t b = lane; b < cap - lo; b += 32) hist[b] = 0;
         __syncwarp();
-        for (int64_t j0 = s; j0 < e && cnt < cap; j0 += 32 * HX_CACHE) {
-            uint32_t uu[HX_CACHE], c1 = 0;
+        for (int64_t j0 = s; j0 < e && cnt < cap; j0 += 32 * HX_STREAM) {
+            uint32_t uu[HX_STREAM], c1 = 0;
 #pragma unroll
-            for (int k = 0; k < HX_CACHE; k++) {
+            for (int k = 0; k < HX_STREAM; k++) {
                 const int64_t j = j0 + k * 32 + lane;
                 uu[k] = j < e ? A.col[j] : 0xffffffffu;
             }
-            uint32_t xx[HX_CACHE];
+            uint32_t xx[HX_STREAM];
 #pragma unroll
-            for (int k = 0; k < HX_CACHE; k++) xx[k] = uu[k] != 0xffffffffu ? __ldcg(&A.c[uu[k]]) : 0u;
+            for (int k = 0; k < HX_STREAM; k++) xx[k] = uu[k] != 0xffffffffu ? __ldcg(&A.c[uu[k]]) : 0u;
 #pragma unroll
-            for (int k = 0; k < HX_CACHE; k++)
+            for (int k = 0; k < HX_STREAM; k++)
                 if (uu[k] != 0xffffffffu) {
                     if (xx[k] >= cap) c1++;
                     else if (xx[k] >= lo) atomicAdd(&hist[xx[k] - lo], 1u);
@@ -249,17 +250,17 @@ __device__ bool hx_warp_vertex(const HxArgs &A, uint32_t v, unsigned cur, bool c
         for (int k = 0; k < HX_CACHE; k++)
             if (cu[k] != 0xffffffffu && cv[k] > h && cv[k] <= cap) hx_activate(A, cu[k], nxt);
     } else {
-        for (int64_t jb = s + lane; jb < e; jb += 32 * HX_CACHE) {
-            uint32_t uu[HX_CACHE], xx[HX_CACHE];
+        for (int64_t jb = s + lane; jb < e; jb += 32 * HX_STREAM) {
+            uint32_t uu[HX_STREAM], xx[HX_STREAM];
 #pragma unroll
-            for (int k = 0; k < HX_CACHE; k++) {
+            for (int k = 0; k < HX_STREAM; k++) {
                 const int64_t j = jb + k * 32;
                 uu[k] = j < e ? A.col[j] : 0xffffffffu;
             }
 #pragma unroll
-            for (int k = 0; k < HX_CACHE; k++) xx[k] = uu[k] != 0xffffffffu ? __ldcg(&A.c[uu[k]]) : 0u;
+            for (int k = 0; k < HX_STREAM; k++) xx[k] = uu[k] != 0xffffffffu ? __ldcg(&A.c[uu[k]]) : 0u;
 #pragma unroll
-            for (int k = 0; k < HX_CACHE; k++)
+            for (int k = 0; k < HX_STREAM; k++)
                 if (uu[k] != 0xffffffffu && xx[k] > h && xx[k] <= cap) hx_activate(A, uu[k], nxt);
         }
     }

@@ -171,16 +171,32 @@ int kc_graph_save(const kc_graph *g, const char *path) {
     const uint64_t n = g->n, nnz = g->nnz;
     const bool with_core = g->core_valid && g->core;
     const uint64_t b_row = (n + 1) * 8, b_col = nnz * 4, pad = (8 - (b_col & 7)) & 7, b_core = with_core ? n * 4 : 0;
-    std::vector<unsigned char> buf;
-    try {
-        buf.resize(b_row + b_col + pad + b_core);
-    } catch (...) {
-        return fail(KC_ERR_NOMEM, "host buffer for the snapshot (%llu bytes)",
-                    (unsigned long long)(b_row + b_col + pad + b_core));
+    // The file is sized first and mapped: the device copies land in its
+    // pages directly (no zero-filled staging buffer, no second copy by a
+    // write call), and the hash is taken from them.
+    const uint64_t payload = b_row + b_col + pad + b_core;
+    const uint64_t total = sizeof(SnapHeader) + payload;
+    const int fd = open(path, O_RDWR | O_CREAT | O_TRUNC, 0644);
+    if (fd < 0) return fail(KC_ERR_IO, "cannot create %s", path);
+    if (ftruncate(fd, (off_t)total) != 0) {
+        close(fd);
+        return fail(KC_ERR_IO, "cannot size %s to %llu bytes", path, (unsigned long long)total);
     }
-    KC_CUDA(cudaMemcpy(buf.data(), g->rowptr, b_row, cudaMemcpyDeviceToHost));
-    if (b_col) KC_CUDA(cudaMemcpy(buf.data() + b_row, g->col, b_col, cudaMemcpyDeviceToHost));
-    if (b_core) KC_CUDA(cudaMemcpy(buf.data() + b_row + b_col + pad, g->core, b_core, cudaMemcpyDeviceToHost));
+    void *map = mmap(nullptr, total, PROT_READ | PROT_WRITE, MAP_SHARED, fd, 0);
+    if (map == MAP_FAILED) {
+        close(fd);
+        return fail(KC_ERR_IO, "cannot map %s for writing", path);
+    }
+    unsigned char *base = (unsigned char *)map + sizeof(SnapHeader);
+    cudaError_t e = cudaMemcpy(base, g->rowptr, b_row, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && b_col) e = cudaMemcpy(base + b_row, g->col, b_col, cudaMemcpyDeviceToHost);
+    if (pad) std::memset(base + b_row + b_col, 0, pad);
+    if (e == cudaSuccess && b_core) e = cudaMemcpy(base + b_row + b_col + pad, g->core, b_core, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) {
+        munmap(map, total);
+        close(fd);
+        return fail(KC_ERR_CUDA, "snapshot download: %s", cudaGetErrorString(e));
+    }
     SnapHeader h;
     std::memset(&h, 0, sizeof(h));
     std::memcpy(h.magic, SNAP_MAGIC, 8);
@@ -188,13 +204,10 @@ int kc_graph_save(const kc_graph *g, const char *path) {
     h.flags = with_core ? SNAP_HAS_CORE : 0u;
     h.n = n;
     h.nnz = nnz;
-    h.hash = content_hash({{buf.data(), buf.size()}});
-    FILE *f = std::fopen(path, "wb");
-    if (!f) return fail(KC_ERR_IO, "cannot create %s", path);
-    bool ok = std::fwrite(&h, sizeof(h), 1, f) == 1;
-    if (ok && !buf.empty()) ok = std::fwrite(buf.data(), 1, buf.size(), f) == buf.size();
-    ok = (std::fclose(f) == 0) && ok;
-    if (!ok) return fail(KC_ERR_IO, "write failed: %s", path);
+    h.hash = content_hash({{base, payload}});
+    std::memcpy(map, &h, sizeof(h));
+    const bool ok = munmap(map, total) == 0;
+    if (close(fd) != 0 || !ok) return fail(KC_ERR_IO, "write failed: %s", path);
     return KC_OK;
 }
 
