@@ -249,3 +249,26 @@ def test_relabelling_and_local_core_property():
         assert np.array_equal(c2[perm], want), method
     g.free()
     h.free()
+
+
+def test_hub_row_above_2_pow_24():
+    """A hub whose row holds more than 2^24 entries (17 M leaves), joined to
+    a 64-clique: every method against Batagelj-Zaversnik (cores 63 on the
+    clique, 1 elsewhere)."""
+    leaves = (1 << 24) + 1000
+    a, b = np.triu_indices(64, 1)
+    s = np.concatenate([np.zeros(leaves, np.uint32), a.astype(np.uint32) + 1 + leaves])
+    d = np.concatenate([np.arange(1, leaves + 1, dtype=np.uint32), b.astype(np.uint32) + 1 + leaves])
+    s = np.concatenate([s, np.zeros(64, np.uint32)])  # the hub also touches every clique vertex
+    d = np.concatenate([d, np.arange(leaves + 1, leaves + 65, dtype=np.uint32)])
+    n = leaves + 65
+    g = pg.Graph.from_edges(s, d, n, dedup=True)
+    rp, col = g.csr()
+    assert int(np.diff(rp)[0]) == leaves + 64
+    core, kmax = oracle.bz(rp, col)
+    assert kmax == 64  # the hub joins the clique's core: 65 vertices of degree >= 64
+    for method in ("peelone_dyn", "peel_dyn", "peelone", "gppeel", "histo", "cnt", "nbr"):
+        got, st = g.decompose(method)
+        assert np.array_equal(got, core), method
+        assert st.kmax == kmax, method
+    g.free()
