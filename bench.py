@@ -563,10 +563,11 @@ def batch_section(pg, device, sptr, steps, warmup, num_graphs=4096, autotune=Tru
     }
 
 
-def serve_section(pg, device, requests, rate_hz):
+def serve_section(pg, device, requests, rate_hz, sweep_rates=(10.0, 50.0, 200.0)):
     """A Poisson stream of edge-update batches (against a resident R-MAT
     scale-22 graph) and decompositions of fresh batch-mix-style graphs,
-    submitted at their arrival times to the continuous-batching server."""
+    submitted at their arrival times to the continuous-batching server; then
+    the same requests at the sweep's other arrival rates."""
     import numpy as np
 
     from pico_gb300 import workloads
@@ -584,6 +585,24 @@ def serve_section(pg, device, requests, rate_hz):
     srv.close()
     base.free()
     lat = np.array([r["latency_ms"] for r in res])
+    # the same requests at other arrival rates (arrival times rescaled), each
+    # against a fresh copy of the resident graph
+    sweep = []
+    for r_hz in sweep_rates:
+        b2 = pg.rmat_graph(22, 16, 2, device=device)
+        s2 = pg.Server(b2, decompose_slots=2, max_batch_graphs=64)
+        scaled = [dict(q, t=q["t"] * rate_hz / r_hz) for q in reqs]
+        t1 = time.perf_counter()
+        res2 = workloads.run_stream(s2, scaled, realtime=True)
+        w2 = time.perf_counter() - t1
+        st2 = s2.stats()
+        s2.close()
+        b2.free()
+        l2 = np.array([x["latency_ms"] for x in res2])
+        sweep.append({"rate_req_s": r_hz, "p50_ms": round(float(np.percentile(l2, 50)), 3),
+                      "p99_ms": round(float(np.percentile(l2, 99)), 3),
+                      "throughput_req_s": round(len(res2) / w2, 2), "max_inflight": int(st2["max_inflight"]),
+                      "failed": int(st2["failed"])})
     upd = [r for q, r in zip(reqs, res) if q["kind"] == "update"]
     dec = [r for q, r in zip(reqs, res) if q["kind"] == "decompose"]
     upd_edges = sum(q["ins"][0].size + q["dels"][0].size for q in reqs if q["kind"] == "update")
@@ -606,7 +625,7 @@ def serve_section(pg, device, requests, rate_hz):
         "throughput_m_edges_s": round((upd_edges + dec_edges) / wall / 1e6, 3),
         "failed": int(st["failed"]), "decompose_launches": int(st["decompose_launches"]),
         "max_inflight": int(st["max_inflight"]), "latency": "submission (arrival) to result on host",
-        "generate_s": round(gen_s, 2),
+        "generate_s": round(gen_s, 2), "rate_sweep": sweep,
     }
 
 
