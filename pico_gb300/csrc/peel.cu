@@ -260,8 +260,11 @@ __global__ void __launch_bounds__(NT, 1024 / NT) peel_kernel(PeelArgs A) {
             if (tid == 0) {
                 int md = 0;
                 unsigned qsize = q_tail - q_head;
-                if (ld_relaxed(&ctl->err) != 0) md = M_EXIT;
-                if (!md && !scan_done && qsize < SCAN_BELOW) {
+                // the error flag is read only when this CTA has no work at
+                // hand: a busy CTA finishes its local work first, and
+                // reading the flag every step would put one more round trip
+                // on the path of every scan tile and processing round
+                if (!scan_done && qsize < SCAN_BELOW) {
                     unsigned long long t = next_tile * TILE;
                     if (t < scan_len) {
                         tile_base = t;
@@ -288,6 +291,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) peel_kernel(PeelArgs A) {
                     md = M_PROC;
                     rounds_sh++;
                 }
+                if (!md && ld_relaxed(&ctl->err) != 0) md = M_EXIT;
                 if (!md) {
                     // idle: hand back the credits held, after publishing this
                     // CTA's level minimum and claim flag
