@@ -36,6 +36,19 @@
 
 namespace kc {
 
+// Work items (64 bits): (v << 32) | c is chunk c of the row of vertex v
+// (c < 2^31); a range item, bit 31 set, carries the row entries
+// [r0, r0 + len) themselves (r0 < 2^40, len < 2^23), so that the CTA taking
+// it needs no load of the row offsets.  Claims made while relaxing a row and
+// the chunks of long rows are range items.
+constexpr uint32_t RANGE_FLAG = 0x80000000u;
+constexpr uint32_t RANGE_LEN = (1u << 23) - 1u;
+__device__ __forceinline__ unsigned long long range_item(int64_t r0, uint32_t len) {
+    return ((unsigned long long)((uint64_t)r0 >> 8) << 32) | RANGE_FLAG | ((uint32_t)(r0 & 0xff) << 23) | len;
+}
+__device__ __forceinline__ bool range_fits(int64_t r0, int64_t r1) {
+    return r1 - r0 <= (int64_t)RANGE_LEN && r1 < ((int64_t)1 << 40) - 1;  // never the all-ones sentinel
+}
 constexpr unsigned LOW_WATER = 1024;  // take a new scan tile only below this queue size
 constexpr unsigned MIN_CHUNK = 256;   // smallest row chunk (sizes the shared queues)
 constexpr unsigned long long SENT = ~0ull;
@@ -536,13 +549,21 @@ __global__ void __launch_bounds__(NT, 1024 / NT) peel_kernel(PeelArgs A) {
                     nit = my_hi > my_lo ? my_hi - my_lo : 0u;
                     if (lane < nit) item = q[(my_lo + lane) % QCAP];
                 }
-                int64_t rs = 0;
+                int64_t rs = 0, r0 = 0, r1 = 0;
                 uint32_t len = 0;
                 bool hub = false;
                 if (item != SENT) {
-                    uint32_t v = (uint32_t)(item >> 32);
-                    uint32_t c = (uint32_t)item;
-                    int64_t r0 = A.rowptr[v], r1 = A.rowptr[v + 1];
+                    const uint32_t lo = (uint32_t)item;
+                    uint32_t c = 0;
+                    if (lo & RANGE_FLAG) {
+                        r0 = (int64_t)(((item >> 32) << 8) | ((lo >> 23) & 0xffu));
+                        r1 = r0 + (lo & RANGE_LEN);
+                    } else {
+                        const uint32_t v = (uint32_t)(item >> 32);
+                        c = lo;
+                        r0 = A.rowptr[v];
+                        r1 = A.rowptr[v + 1];
+                    }
                     rs = r0 + (int64_t)c * A.chunk;
                     int64_t re = min(r1, rs + (int64_t)A.chunk);
                     len = re > rs ? (uint32_t)(re - rs) : 0u;
@@ -584,9 +605,9 @@ __global__ void __launch_bounds__(NT, 1024 / NT) peel_kernel(PeelArgs A) {
                 while (hubs) {
                     const int srcl = __ffs(hubs) - 1;
                     hubs &= hubs - 1;
-                    unsigned long long hi = __shfl_sync(KC_FULL_MASK, item, srcl);
-                    uint32_t v = (uint32_t)(hi >> 32);
-                    int64_t d = A.rowptr[v + 1] - A.rowptr[v];
+                    const int64_t h0 = __shfl_sync(KC_FULL_MASK, r0, srcl);
+                    const int64_t h1 = __shfl_sync(KC_FULL_MASK, r1, srcl);
+                    const int64_t d = h1 - h0;
                     unsigned k = (unsigned)((d + A.chunk - 1) / A.chunk);
                     unsigned extra = k - 1;
                     // spread the chunks over the shared queues, 32 per queue
@@ -604,9 +625,13 @@ __global__ void __launch_bounds__(NT, 1024 / NT) peel_kernel(PeelArgs A) {
                             if (A.trace && li < A.trace_cap) atomicAdd(&A.trace[li].spilled, cnt);
                         }
                         pos = __shfl_sync(KC_FULL_MASK, pos, 0);
-                        if (lane < cnt && pos + cnt <= A.gq_cap)
+                        if (lane < cnt && pos + cnt <= A.gq_cap) {
+                            // chunk c0 + lane + 1 as a range item
+                            const int64_t cs = h0 + (int64_t)(c0 + lane + 1) * A.chunk;
+                            const int64_t ce = min(h1, cs + (int64_t)A.chunk);
                             st_relaxed64(&A.gq[((unsigned long long)s * A.nq + qi) * A.gq_cap + pos + lane],
-                                         ((unsigned long long)v << 32) | (c0 + lane + 1));
+                                         range_item(cs, (uint32_t)(ce - cs)));
+                        }
                     }
                 }
                 // expand the rows; each thread keeps PEEL_U entries in flight
@@ -667,13 +692,19 @@ __global__ void __launch_bounds__(NT, 1024 / NT) peel_kernel(PeelArgs A) {
                     for (int k = 0; k < PEEL_U; k++) a[k] = live[k] ? atomicSub(&A.deg[u[k]], 1u) : 0u;
                     // the decrement that moved u from L+1 to L claims it; the
                     // claim atomics of all PEEL_U entries are in flight together
+                    // (with the row offsets of each candidate, so that its row
+                    // can be queued as a range item)
                     unsigned oldc[PEEL_U];
+                    int64_t cr0[PEEL_U], cr1[PEEL_U];
 #pragma unroll
                     for (int k = 0; k < PEEL_U; k++) {
                         oldc[k] = ~0u;
+                        cr0[k] = cr1[k] = 0;
                         if (live[k]) {
                             if (a[k] == L + 1) {
                                 oldc[k] = atomicOr(&A.claimed[u[k] >> 5], 1u << (u[k] & 31));
+                                cr0[k] = A.rowptr[u[k]];
+                                cr1[k] = A.rowptr[u[k] + 1];
                             } else if ((int)a[k] <= (int)L) {
                                 atomicAdd(&A.deg[u[k]], 1u);
                             } else {
@@ -720,7 +751,9 @@ __global__ void __launch_bounds__(NT, 1024 / NT) peel_kernel(PeelArgs A) {
                             slot_hi = __shfl_sync(KC_FULL_MASK, slot_hi, 0);
                             const unsigned r = __popc(pb & ((1u << lane) - 1u));
                             if (push) {
-                                const unsigned long long itm = (unsigned long long)u[k] << 32;
+                                const unsigned long long itm = range_fits(cr0[k], cr1[k])
+                                                                   ? range_item(cr0[k], (uint32_t)(cr1[k] - cr0[k]))
+                                                                   : (unsigned long long)u[k] << 32;
                                 if (spill == 0)
                                     q[(slot_lo + r) % QCAP] = itm;
                                 else if (spill == 1)
