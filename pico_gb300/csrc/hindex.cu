@@ -115,6 +115,56 @@ __device__ __forceinline__ void hx_activate(const HxArgs &A, uint32_t u, unsigne
     }
 }
 
+// hx_activate for K candidates per lane (u[k] where cand[k]), warp-wide:
+// every lane calls it.  The pending-bit reads, the claiming atomicOr, the
+// row-length reads and the list appends of all K candidates are each in
+// flight together, and the appends to each list take one atomicAdd per warp.
+template <int K>
+__device__ __forceinline__ void hx_activate_all(const HxArgs &A, const uint32_t (&u)[K], const bool (&cand)[K],
+                                                unsigned nxt, unsigned lane) {
+    bool anyc = false;
+#pragma unroll
+    for (int k = 0; k < K; k++) anyc |= cand[k];
+    if (!__any_sync(KC_FULL_MASK, anyc)) return;
+    bool need[K];
+#pragma unroll
+    for (int k = 0; k < K; k++)
+        need[k] = cand[k] && !(__ldcg(&A.inlist[nxt][u[k] >> 5]) & (1u << (u[k] & 31)));
+    unsigned old[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) old[k] = need[k] ? atomicOr(&A.inlist[nxt][u[k] >> 5], 1u << (u[k] & 31)) : ~0u;
+    int kind[K];  // -1: nothing to queue; 0 short, 1 medium, 2 long row
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        kind[k] = -1;
+        if (!(old[k] & (1u << (u[k] & 31)))) {
+            const int64_t d = A.rowptr[u[k] + 1] - A.rowptr[u[k]];
+            kind[k] = d > (int64_t)A.warp_rows ? 2 : d > (int64_t)HX_WARP_MAX ? 1 : 0;
+        }
+    }
+    const unsigned lt = (1u << lane) - 1u;
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        if (!__any_sync(KC_FULL_MASK, kind[k] >= 0)) continue;
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+            const unsigned m = __ballot_sync(KC_FULL_MASK, kind[k] == q);
+            if (!m) continue;
+            unsigned long long base = 0;
+            if (lane == __ffs(m) - 1)
+                base = atomicAdd(q == 2 ? &A.ctl->big_len[nxt] : q == 1 ? &A.ctl->mid_len[nxt] : &A.ctl->list_len[nxt],
+                                 (unsigned long long)__popc(m));
+            base = __shfl_sync(KC_FULL_MASK, base, __ffs(m) - 1);
+            if (kind[k] == q) {
+                const unsigned long long p = base + __popc(m & lt);
+                if (q == 2) A.big[nxt][p] = u[k];
+                else if (q == 1) A.list[nxt][A.n - p] = u[k];
+                else A.list[nxt][p] = u[k];
+            }
+        }
+    }
+}
+
 // The largest k in [max(lo, 1), hi] with count(>= k) >= k, from the window
 // hist[k - lo] whose top bin hi - lo counts every value at or above hi; -1 if
 // none qualifies, and then carry = count(>= max(lo, 1)).
@@ -246,22 +296,24 @@ __device__ bool hx_warp_vertex(const HxArgs &A, uint32_t v, unsigned cur, bool c
     // can differ only if u was lowered concurrently in this sweep, and such a
     // u re-examines itself in the next sweep (below), after this write.
     if (cached) {
+        bool cand[HX_CACHE];
 #pragma unroll
-        for (int k = 0; k < HX_CACHE; k++)
-            if (cu[k] != 0xffffffffu && cv[k] > h && cv[k] <= cap) hx_activate(A, cu[k], nxt);
+        for (int k = 0; k < HX_CACHE; k++) cand[k] = cu[k] != 0xffffffffu && cv[k] > h && cv[k] <= cap;
+        hx_activate_all(A, cu, cand, nxt, lane);
     } else {
-        for (int64_t jb = s + lane; jb < e; jb += 32 * HX_STREAM) {
+        for (int64_t jw = s; jw < e; jw += 32 * HX_STREAM) {  // warp-uniform trip count
             uint32_t uu[HX_STREAM], xx[HX_STREAM];
 #pragma unroll
             for (int k = 0; k < HX_STREAM; k++) {
-                const int64_t j = jb + k * 32;
+                const int64_t j = jw + k * 32 + lane;
                 uu[k] = j < e ? A.col[j] : 0xffffffffu;
             }
 #pragma unroll
             for (int k = 0; k < HX_STREAM; k++) xx[k] = uu[k] != 0xffffffffu ? __ldcg(&A.c[uu[k]]) : 0u;
+            bool cand[HX_STREAM];
 #pragma unroll
-            for (int k = 0; k < HX_STREAM; k++)
-                if (uu[k] != 0xffffffffu && xx[k] > h && xx[k] <= cap) hx_activate(A, uu[k], nxt);
+            for (int k = 0; k < HX_STREAM; k++) cand[k] = uu[k] != 0xffffffffu && xx[k] > h && xx[k] <= cap;
+            hx_activate_all(A, uu, cand, nxt, lane);
         }
     }
     // A neighbour lowered in this sweep may have read c[v] before this write
@@ -346,13 +398,12 @@ __device__ unsigned hx_warp_tiny(const HxArgs &A, uint32_t vg, bool valid, unsig
     const bool low = act && h < cap;
     if (low && gl == 0) A.c[vg] = h;
     __syncwarp();
-    if (low) {
-        // notification window and self-requeue as in hx_warp_vertex
+    // notification window and self-requeue as in hx_warp_vertex
+    bool cand[4];
 #pragma unroll
-        for (int k = 0; k < 4; k++)
-            if (cu[k] != 0xffffffffu && cv[k] > h && cv[k] <= cap) hx_activate(A, cu[k], nxt);
-        if (gl == 0) hx_activate(A, vg, nxt);
-    }
+    for (int k = 0; k < 4; k++) cand[k] = low && cu[k] != 0xffffffffu && cv[k] > h && cv[k] <= cap;
+    hx_activate_all(A, cu, cand, nxt, lane);
+    if (low && gl == 0) hx_activate(A, vg, nxt);
     return (unsigned)__popc(__ballot_sync(KC_FULL_MASK, low && gl == 0));
 }
 
@@ -501,18 +552,23 @@ __device__ bool hx_block_vertex(const HxArgs &A, uint32_t v, unsigned nxt, uint3
     if (threadIdx.x == 0) A.c[v] = h;
     __syncthreads();
     // notification window and self-requeue as in hx_warp_vertex
-    for (int64_t jb = s + threadIdx.x; jb < e; jb += HX_CACHE * HX_THREADS) {
-        uint32_t uu[HX_CACHE], xx[HX_CACHE];
+    {
+        const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        // warp-uniform blocks of 32 * HX_CACHE entries
+        for (int64_t jw = s + (int64_t)warp * 32 * HX_CACHE; jw < e; jw += (int64_t)HX_THREADS * HX_CACHE) {
+            uint32_t uu[HX_CACHE], xx[HX_CACHE];
 #pragma unroll
-        for (int k = 0; k < HX_CACHE; k++) {
-            const int64_t j = jb + k * HX_THREADS;
-            uu[k] = j < e ? A.col[j] : 0xffffffffu;
+            for (int k = 0; k < HX_CACHE; k++) {
+                const int64_t j = jw + k * 32 + lane;
+                uu[k] = j < e ? A.col[j] : 0xffffffffu;
+            }
+#pragma unroll
+            for (int k = 0; k < HX_CACHE; k++) xx[k] = uu[k] != 0xffffffffu ? __ldcg(&A.c[uu[k]]) : 0u;
+            bool cand[HX_CACHE];
+#pragma unroll
+            for (int k = 0; k < HX_CACHE; k++) cand[k] = uu[k] != 0xffffffffu && xx[k] > h && xx[k] <= cap;
+            hx_activate_all(A, uu, cand, nxt, lane);
         }
-#pragma unroll
-        for (int k = 0; k < HX_CACHE; k++) xx[k] = uu[k] != 0xffffffffu ? __ldcg(&A.c[uu[k]]) : 0u;
-#pragma unroll
-        for (int k = 0; k < HX_CACHE; k++)
-            if (uu[k] != 0xffffffffu && xx[k] > h && xx[k] <= cap) hx_activate(A, uu[k], nxt);
     }
     if (threadIdx.x == 0) hx_activate(A, v, nxt);
     __syncthreads();
