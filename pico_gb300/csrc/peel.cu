@@ -171,9 +171,10 @@ __global__ void __launch_bounds__(NT, 1024 / NT) peel_kernel(PeelArgs A) {
     constexpr unsigned TILE = NT * SCAN_U;
     __shared__ unsigned long long q[QCAP];
     __shared__ unsigned int q_head, q_tail;
+    __shared__ unsigned int q_res;  // scan: queue slots reserved so far in this tile
     __shared__ int mode;
     __shared__ unsigned int b_base, b_per_warp, b_take;
-    __shared__ unsigned long long tile_base, scan_len, out_base;
+    __shared__ unsigned long long tile_base, scan_len;
     __shared__ unsigned int scan_done;
     __shared__ unsigned long long credit;
     __shared__ unsigned int min_sh, claimed_any;
@@ -181,8 +182,6 @@ __global__ void __launch_bounds__(NT, 1024 / NT) peel_kernel(PeelArgs A) {
     __shared__ unsigned int steal_cnt, probe, claims_sh, spill_rr;
     __shared__ unsigned int level_sh, li_sh;
     __shared__ unsigned long long wait_t0;
-    __shared__ unsigned int warp_cnt[SCAN_U][PEEL_WARPS];   // scan: survivors per warp
-    __shared__ unsigned int warp_push[SCAN_U][PEEL_WARPS];  // scan: claims per warp
     __shared__ unsigned long long next_tile;
     __shared__ unsigned int withheld;
     __shared__ unsigned int rounds_sh;
@@ -282,6 +281,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) peel_kernel(PeelArgs A) {
                     if (t < scan_len) {
                         tile_base = t;
                         next_tile += G;
+                        q_res = q_tail;
                         md = M_SCAN;
                     } else {
                         scan_done = 1;
@@ -431,7 +431,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) peel_kernel(PeelArgs A) {
                 // ---- scan one tile (SCAN_U entries per thread) of the alive list
                 uint32_t v[SCAN_U];
                 unsigned d[SCAN_U];
-                bool inr[SCAN_U], keep[SCAN_U], take[SCAN_U], push[SCAN_U];
+                bool inr[SCAN_U], keep[SCAN_U];
 #pragma unroll
                 for (int k = 0; k < SCAN_U; k++) {
                     const unsigned long long pos = tile_base + (unsigned)k * PEEL_THREADS + tid;
@@ -453,6 +453,8 @@ __global__ void __launch_bounds__(NT, 1024 / NT) peel_kernel(PeelArgs A) {
                 // atomics are issued before any result is used
                 unsigned oldw[SCAN_U];
                 int leader[SCAN_U];
+                unsigned kb[SCAN_U];
+                unsigned kcnt = 0;
 #pragma unroll
                 for (int k = 0; k < SCAN_U; k++) {
                     keep[k] = inr[k] && (int)d[k] > (int)L;
@@ -465,68 +467,47 @@ __global__ void __launch_bounds__(NT, 1024 / NT) peel_kernel(PeelArgs A) {
                     leader[k] = __ffs(peers) - 1;
                     oldw[k] = 0;
                     if (want && (int)lane == leader[k]) oldw[k] = atomicOr(&A.claimed[word], bits);
+                    kb[k] = __ballot_sync(KC_FULL_MASK, keep[k]);
+                    kcnt += __popc(kb[k]);
                 }
+                // survivors: each warp reserves its run of the next alive list
+                // with one atomicAdd, in flight with the claim atomics
+                unsigned long long wbase = 0;
+                if (lane == 0 && kcnt) wbase = atomicAdd(&ctl->out_len[s], (unsigned long long)kcnt);
                 dkeep = __reduce_min_sync(KC_FULL_MASK, dkeep);
                 if (lane == 0 && dkeep != NO_LEVEL) atomicMin(&min_sh, dkeep);
-                // survivors first: their count reserves space in the next list
-                // while the claim atomics are still in flight
-                unsigned kb[SCAN_U], cb[SCAN_U];
-#pragma unroll
-                for (int k = 0; k < SCAN_U; k++) {
-                    kb[k] = __ballot_sync(KC_FULL_MASK, keep[k]);
-                    if (lane == 0) warp_cnt[k][warp] = __popc(kb[k]);
-                }
-                __syncthreads();
-                // offsets: sub-tiles in order, warps in order within a sub-tile
-                unsigned ktot = 0;
-                unsigned kofs[SCAN_U];
-#pragma unroll
-                for (int k = 0; k < SCAN_U; k++) {
-                    kofs[k] = ktot;
-                    for (unsigned w2 = 0; w2 < PEEL_WARPS; w2++) {
-                        const unsigned x = warp_cnt[k][w2];
-                        if (w2 < warp) kofs[k] += x;
-                        ktot += x;
-                    }
-                }
-                if (tid == 0 && ktot) out_base = atomicAdd(&ctl->out_len[s], (unsigned long long)ktot);
-                unsigned any_take = 0;
+                unsigned cb[SCAN_U];
+                unsigned ccnt = 0;
 #pragma unroll
                 for (int k = 0; k < SCAN_U; k++) {
                     const unsigned old = __shfl_sync(KC_FULL_MASK, oldw[k], leader[k]);
-                    take[k] = inr[k] && !keep[k] && !(old & (1u << (v[k] & 31)));
+                    const bool take = inr[k] && !keep[k] && !(old & (1u << (v[k] & 31)));
                     // listed vertices have non-empty rows (the degree-0 ones
                     // are peeled by peel_init), so every claim is queued
-                    push[k] = take[k];
-                    cb[k] = __ballot_sync(KC_FULL_MASK, push[k]);
-                    any_take += __popc(cb[k]);
-                    if (lane == 0) warp_push[k][warp] = __popc(cb[k]);
+                    cb[k] = __ballot_sync(KC_FULL_MASK, take);
+                    ccnt += __popc(cb[k]);
                 }
-                if (lane == 0 && any_take) {
+                // claims: each warp reserves queue slots in shared memory (the
+                // tile was taken only while the queue had room for all of them)
+                unsigned qb = 0;
+                if (lane == 0 && ccnt) qb = atomicAdd(&q_res, ccnt);
+                if (lane == 0 && ccnt) {
                     claimed_any = 1;
-                    if (A.trace) atomicAdd(&claims_sh, any_take);
+                    if (A.trace) atomicAdd(&claims_sh, ccnt);
                 }
-                __syncthreads();
-                unsigned ctot = 0;
-                unsigned cofs[SCAN_U];
-#pragma unroll
-                for (int k = 0; k < SCAN_U; k++) {
-                    cofs[k] = ctot;
-                    for (unsigned w2 = 0; w2 < PEEL_WARPS; w2++) {
-                        const unsigned x = warp_push[k][w2];
-                        if (w2 < warp) cofs[k] += x;
-                        ctot += x;
-                    }
-                }
+                wbase = __shfl_sync(KC_FULL_MASK, wbase, 0);
+                qb = __shfl_sync(KC_FULL_MASK, qb, 0);
                 const unsigned lt = (1u << lane) - 1u;
+                unsigned ko = 0, co = 0;
 #pragma unroll
                 for (int k = 0; k < SCAN_U; k++) {
-                    if (keep[k]) dst[out_base + kofs[k] + __popc(kb[k] & lt)] = v[k];
-                    if (push[k]) q[(q_tail + cofs[k] + __popc(cb[k] & lt)) % QCAP] = ((unsigned long long)v[k] << 32);
+                    if (keep[k]) dst[wbase + ko + __popc(kb[k] & lt)] = v[k];
+                    if (cb[k] & (1u << lane)) q[(qb + co + __popc(cb[k] & lt)) % QCAP] = ((unsigned long long)v[k] << 32);
+                    ko += __popc(kb[k]);
+                    co += __popc(cb[k]);
                 }
                 __syncthreads();
-                if (tid == 0) q_tail += ctot;
-                __syncthreads();
+                if (tid == 0) q_tail = q_res;
                 continue;
             }
 
