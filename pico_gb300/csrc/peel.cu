@@ -190,7 +190,6 @@ __global__ void __launch_bounds__(NT, 1024 / NT) peel_kernel(PeelArgs A) {
     __shared__ unsigned int bal_off[BAL ? NT + 1 : 1];  // balanced rounds: item offsets,
     __shared__ int64_t bal_rs[BAL ? NT : 1];            // row starts,
     __shared__ unsigned int bal_wsum[NT / 32];          // per-warp sums
-    __shared__ unsigned int bal_take;                   // and item count
 
     const unsigned tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const unsigned G = gridDim.x;
@@ -519,6 +518,10 @@ __global__ void __launch_bounds__(NT, 1024 / NT) peel_kernel(PeelArgs A) {
             // never outlasts a few dependent memory round trips and a claim
             // made in it is picked up in the next round.
             {
+                // the CTA queue's head once this round's items are taken (the
+                // spill threshold counts the items queued behind it)
+                unsigned round_head = q_head;
+                unsigned bal_n = 0;  // balanced rounds: items taken
                 unsigned long long item = SENT;
                 unsigned nit;
                 if constexpr (BAL) {
@@ -564,22 +567,23 @@ __global__ void __launch_bounds__(NT, 1024 / NT) peel_kernel(PeelArgs A) {
                         ctot += x;
                     }
                     off += wbase;
-                    // the items that start within the budget (a prefix)
+                    // the items that start within the budget (a prefix); each
+                    // writes its start and, at the next index, its end (the
+                    // next item's start: the same value), so the barrier that
+                    // counts them also publishes the offsets
                     const bool inb = nit && off < A.round_e;
-                    const unsigned take = (unsigned)__syncthreads_count(inb);
                     if (inb) {
                         bal_off[tid] = off;
+                        bal_off[tid + 1] = off + len;
                         bal_rs[tid] = rs;
                     }
-                    if (tid + 1 == take) bal_off[take] = off + len;
-                    if (tid == 0) {
-                        q_head = b_base + take;  // the rest stays queued
-                        bal_take = take;
-                    }
+                    const unsigned take = (unsigned)__syncthreads_count(inb);
+                    bal_n = take;
+                    round_head = b_base + take;  // the rest stays queued
+                    if (tid == 0) q_head = round_head;
                     hub = hub && inb;
                     (void)ctot;
-                    __syncthreads();
-                    total = bal_off[bal_take];
+                    total = bal_off[take];
                 }
                 // split hub rows: chunk items 1..k-1 go to the global queue
                 unsigned hubs = __ballot_sync(KC_FULL_MASK, hub);
@@ -635,7 +639,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) peel_kernel(PeelArgs A) {
                         live[k] = e < total;
                         if constexpr (BAL) {
                             // owner item: the last j with bal_off[j] <= e
-                            unsigned lo = 0, hi2 = bal_take;
+                            unsigned lo = 0, hi2 = bal_n;
                             if (live[k]) {
                                 while (hi2 - lo > 1) {
                                     const unsigned mid = (lo + hi2) >> 1;
@@ -709,7 +713,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) peel_kernel(PeelArgs A) {
                             if (lane == 0) {
                                 unsigned t = q_tail;
                                 for (;;) {
-                                    if (t + cnt - b_base > QCAP || t + cnt - q_head > A.spill_t) { spill = 1; break; }
+                                    if (t + cnt - b_base > QCAP || t + cnt - round_head > A.spill_t) { spill = 1; break; }
                                     unsigned old = atomicCAS(&q_tail, t, t + cnt);
                                     if (old == t) break;
                                     t = old;
