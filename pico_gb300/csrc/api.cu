@@ -565,7 +565,8 @@ int kc_graph_set_param(kc_graph *g, const char *name, int64_t value) {
     std::string k(name);
     Tuning &t = g->tune;
     if (k == "peel.chunk") {
-        if (value < 256 || value > (1 << 20) || (value & (value - 1))) return fail(KC_ERR_INVALID, "peel.chunk: power of two in [256, 2^20]");
+        if (value != 0 && (value < 256 || value > (1 << 20) || (value & (value - 1))))
+            return fail(KC_ERR_INVALID, "peel.chunk: 0 (by graph size) or a power of two in [256, 2^20]");
         t.peel_chunk = (int)value;
     } else if (k == "peel.spill") {
         if (value < 0 || value > 3072) return fail(KC_ERR_INVALID, "peel.spill: [0, 3072]");

@@ -97,7 +97,7 @@ struct PeelTrace {
 };
 
 struct Tuning {
-    int peel_chunk = 1024;
+    int peel_chunk = 0;  // 0: by graph size (1024 entries, 2048 from 2^29 entries up)
     int peel_spill = 32;
     int peel_steal = 64;
     int peel_queues = 1;

@@ -889,7 +889,9 @@ int peel_run(Graph *g, cudaStream_t s, bool gpp_zero_to_one_flag, kc_stats *st) 
     A.timeout_ns = (unsigned long long)g->tune.wait_timeout_us * 1000ull;
     A.withhold = (unsigned)g->tune.withhold;
     A.max_level_indices = g->max_deg + 3;
-    A.chunk = (unsigned)g->tune.peel_chunk;
+    // measured: 1024-entry chunks on R-MAT scale 22 (128 M entries), 2048 on
+    // R-MAT scale 25 (1.07 B entries, 4% faster than 1024)
+    A.chunk = g->tune.peel_chunk ? (unsigned)g->tune.peel_chunk : (g->nnz >= (1ull << 29) ? 2048u : 1024u);
     A.spill_t = (unsigned)g->tune.peel_spill;
     A.steal_max = (unsigned)g->tune.peel_steal;
     A.nq = nq_of(g);
