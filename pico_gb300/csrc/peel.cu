@@ -6,13 +6,15 @@
 //
 // State per vertex: deg[v] (residual degree; equals the core number when the
 // kernel returns) and one bit in `claimed` (v has been peeled).  Per level L:
-//   * scan: CTAs take 512-vertex tiles of the global list of still-alive
-//     vertices from a shared cursor, claim those with deg <= L (atomicOr on
-//     the claim bit decides a unique owner), append the survivors to the next
-//     level's list (one atomicAdd per tile) and record min(deg) of them;
-//   * process: a claimed vertex's row is walked by one warp, several short
-//     rows per warp through a shuffle-based load balance; rows above CHUNK
-//     entries are split into chunk items that any CTA may take.  Each
+//   * scan: CTA b takes tiles b, b + G, b + 2G, ... (threads x SCAN_U
+//     entries each) of the list of still-alive vertices, claims those with
+//     deg <= L (atomicOr on the claim bit decides a unique owner), appends
+//     the survivors to the next level's list and the claims to its queue
+//     (one reservation per warp) and records min(deg) of the survivors;
+//   * process: balanced rounds spread the row entries of the queued items
+//     (up to round_e of them) over all threads of the CTA; rows above CHUNK
+//     entries are split into chunk items that any CTA may take, and the
+//     claims made while relaxing carry their row range in the item.  Each
 //     unclaimed neighbour u gets atomicSub(deg[u]); the thread that moves u
 //     from L+1 to L claims it and queues it, so sub-level cascades run inside
 //     the level without grid synchronisation (the reference repeats the level
