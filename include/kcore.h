@@ -193,7 +193,8 @@ int kc_graph_last_timing(const kc_graph *g, double *total_ms, double *kernel_ms)
  * the benchmarks use these).  Names: "peel.chunk" (row entries per peel work
  * item; 0, the default, picks 1024, or 2048 for graphs of 2^29 entries or
  * more), "peel.spill" (cascade items a CTA keeps before publishing to the
- * shared queues), "peel.steal" (most items reserved per steal, 1..64), "peel.queues" (number
+ * shared queues, default 16), "peel.steal" (most items reserved per steal,
+ * 1..64, default 32), "peel.queues" (number
  * of shared queues, 1..64), "peel.ctas_per_sm" (0 = occupancy maximum),
  * "peel.unroll" (row entries each lane keeps in flight, 4 or 8),
  * "peel.threads" (threads per CTA, 512 or 256), "peel.balanced" (1 = each

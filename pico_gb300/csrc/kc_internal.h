@@ -98,8 +98,8 @@ struct PeelTrace {
 
 struct Tuning {
     int peel_chunk = 0;  // 0: by graph size (1024 entries, 2048 from 2^29 entries up)
-    int peel_spill = 32;
-    int peel_steal = 64;
+    int peel_spill = 16;  // measured best with 32-item steals (R-MAT scale 22 and 25)
+    int peel_steal = 32;
     int peel_queues = 1;
     int peel_ctas_per_sm = 0;
     int peel_unroll = 4;  // row entries in flight per lane: 4 or 8
