@@ -47,7 +47,7 @@ enum {
 
 /* Decomposition methods: the seven reference drivers plus automatic choice.
  * All produce the exact core numbers; KC_GPP additionally reports core 1 for
- * degree-0 vertices, as peel/gppeel.cu:247-252 does. */
+ * degree-0 vertices, as peel/gppeel.cu:35-39 does. */
 enum {
     KC_HISTO = 0,       /* index2core/HistoCore.cu   h-index iteration        */
     KC_CNT = 1,         /* index2core/CntCore.cu     h-index iteration        */
@@ -178,8 +178,8 @@ int kc_graph_virtual_layout(kc_graph *g, uint32_t part_size, uint32_t *node_poin
 /* ---- decomposition ----------------------------------------------------- */
 /* Core number of every vertex.  Replaces the timed loops of HistoCore.cu:292-341,
  * CntCore.cu:344-417, NbrCore.cu:244-297, peelone.cu:157-186,
- * gppeel.cu:398-440, int peelone_dyn(Graph&) (peelone-dyn.cc:120-168) and
- * int peel_dyn(Graph&) (peel-dyn.cc:301-350).  core_out: n uint32 in host
+ * gppeel.cu:186-228, int peelone_dyn(Graph&) (peelone-dyn.cc:120-168) and
+ * int peel_dyn(Graph&) (peel-dyn.cc:133-182).  core_out: n uint32 in host
  * memory (out_on_device = 0) or device memory of the graph's device
  * (out_on_device = 1); may be NULL to keep the result on the device only
  * (see kc_graph_device_core).  stats may be NULL. */

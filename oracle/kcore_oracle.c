@@ -203,10 +203,10 @@ int orc_peel_rounds(uint32_t n, const int64_t *rowptr, const uint32_t *col, uint
     return ORC_OK;
 }
 
-/* GPP peel of gppeel.cu:398-440: per round, scan_nodes deletes every live
+/* GPP peel of gppeel.cu:186-228: per round, scan_nodes deletes every live
  * vertex with residual degree <= level and records final_core = level, then
  * scatter_edges decrements each live neighbour without clamping.  Because
- * the first level is 1, degree-0 vertices get core 1 (gppeel.cu:247-252).  */
+ * the first level is 1, degree-0 vertices get core 1 (gppeel.cu:35-39).  */
 int orc_gpp(uint32_t n, const int64_t *rowptr, const uint32_t *col, uint32_t *final_core,
             uint32_t *rounds)
 {

@@ -1,4 +1,4 @@
-// gppeel: drop-in for the reference's gppeel binary (peel/gppeel.cu:320-468).
+// gppeel: drop-in for the reference's gppeel binary (peel/gppeel.cu:108-260).
 // Usage: gppeel <graph.mtx>; prints the reference's report lines.  Set
 // KCORE_OUTPUT=<file> to also write "i core" lines (utility::SaveResults).
 #include "_common.h"

@@ -389,10 +389,34 @@ static void free_classes(kc_batch *b) {
     b->planned = false;
 }
 
+// Raises the dynamic shared-memory limit of batch_peel<DegT, SMEM> on the
+// current device to the opt-in maximum, once per device.  The limit is never
+// lowered afterwards, so a launch planned for one size stays valid whatever
+// other launches of the same kernel (a later plan, the allocation-free entry
+// point, another host thread) need.
+template <typename DegT, bool SMEM>
+static int batch_smem_limit() {
+    static std::mutex mu;
+    static bool done[64] = {};
+    int dev = 0;
+    KC_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return fail(KC_ERR_INVALID, "device %d out of range", dev);
+    std::lock_guard<std::mutex> lk(mu);
+    if (done[dev]) return KC_OK;
+    auto fn = batch_peel<DegT, SMEM>;
+    int optin = 0;
+    KC_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    cudaFuncAttributes fa;
+    KC_CUDA(cudaFuncGetAttributes(&fa, fn));
+    KC_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
+    done[dev] = true;
+    return KC_OK;
+}
+
 template <typename DegT, bool SMEM>
 static int class_grid(int threads, size_t smem, int sms, int *grid) {
     auto fn = batch_peel<DegT, SMEM>;
-    if (smem > 48 * 1024) KC_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (smem > 48 * 1024) KC_TRY((batch_smem_limit<DegT, SMEM>()));
     int occ = 0;
     KC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, threads, smem));
     if (occ < 1) return fail(KC_ERR_UNSUPPORTED, "batch kernel (%d threads, %zu B shared) cannot be resident", threads, smem);
@@ -792,7 +816,7 @@ constexpr uint64_t NOALLOC_WORDS = NOALLOC_CTRL_WORDS + NOALLOC_QUEUE;  // 8-byt
 static __device__ __align__(256) unsigned long long g_noalloc_scratch[NOALLOC_WORDS];
 
 // Writes the one-graph work list into the control block: vbase = {0, n},
-// order = {0}, fbase = {0}, work counter = 0.
+// order = {0}, fbase = {0}, work counter = 0, bad-entry count = 0.
 __global__ void noalloc_prep(unsigned long long *scratch, uint32_t n) {
     uint32_t *w = reinterpret_cast<uint32_t *>(scratch);
     w[0] = 0;  // vbase[0]
@@ -800,6 +824,23 @@ __global__ void noalloc_prep(unsigned long long *scratch, uint32_t n) {
     w[2] = 0;  // order[0]
     w[4] = 0;  // next (work counter)
     scratch[3] = 0ull;  // fbase[0]
+    w[8] = 0;  // entries that fail noalloc_check
+}
+
+// Counts, into control word 8, the row offsets that decrease (or a negative
+// rowptr[0]) and the column ids >= n among col[0, nnz): the kernel indexes its
+// shared-memory arrays by column id, so a caller's bad id must be turned into
+// an error before it runs.
+__global__ void noalloc_check(const int64_t *__restrict__ rowptr, const uint32_t *__restrict__ col, uint32_t n,
+                              uint64_t nnz, unsigned long long *scratch) {
+    unsigned bad = 0;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t t0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    for (uint64_t v = t0; v < n; v += stride) bad += (rowptr[v + 1] < rowptr[v]) ? 1u : 0u;
+    if (t0 == 0 && rowptr[0] < 0) bad++;
+    for (uint64_t e = t0; e < nnz; e += stride) bad += (col[e] >= n) ? 1u : 0u;
+    bad = __reduce_add_sync(KC_FULL_MASK, bad);
+    if ((threadIdx.x & 31) == 0 && bad) atomicAdd(reinterpret_cast<uint32_t *>(scratch) + 8, bad);
 }
 
 static std::mutex g_noalloc_mu;
@@ -816,9 +857,7 @@ static int noalloc_setup(int dev, unsigned long long **out) {
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess || !p)
             return fail(KC_ERR_CUDA, "cudaGetSymbolAddress(no-alloc scratch): %s", cudaGetErrorString(e));
-        const size_t smem = ((NOALLOC_MAX_N * sizeof(uint32_t) + 15) & ~size_t(15)) + ((NOALLOC_MAX_N + 31) / 32) * 4 + 16;
-        e = cudaFuncSetAttribute(batch_peel<uint32_t, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return fail(KC_ERR_CUDA, "no-alloc kernel setup: %s", cudaGetErrorString(e));
+        KC_TRY((batch_smem_limit<uint32_t, true>()));
         g_noalloc_ptr[dev] = p;
     }
     *out = static_cast<unsigned long long *>(g_noalloc_ptr[dev]);
@@ -831,7 +870,7 @@ extern "C" int kc_decompose_noalloc(const int64_t *d_rowptr, const uint32_t *d_c
                                     void *stream) {
     using namespace kc;
     clear_error();
-    if (!d_rowptr || !d_core || (n && !d_col)) return fail(KC_ERR_INVALID, "null argument");
+    if (!d_rowptr || !d_core) return fail(KC_ERR_INVALID, "null argument");
     if (n > NOALLOC_MAX_N)
         return fail(KC_ERR_CAPACITY, "kc_decompose_noalloc: %u vertices exceed the limit of %u", n, NOALLOC_MAX_N);
     int dev = 0;
@@ -846,7 +885,22 @@ extern "C" int kc_decompose_noalloc(const int64_t *d_rowptr, const uint32_t *d_c
         return fail(KC_ERR_CAPACITY, "kc_decompose_noalloc: %lld entries exceed the limit of %llu", (long long)nnz,
                     (unsigned long long)NOALLOC_MAX_NNZ);
     if (n == 0) return KC_OK;
+    if (nnz > 0 && !d_col) return fail(KC_ERR_INVALID, "null column array with %lld entries", (long long)nnz);
     noalloc_prep<<<1, 1, 0, s>>>(scratch, n);
+    {
+        const uint64_t work = std::max<uint64_t>((uint64_t)nnz, n);
+        const unsigned blocks = (unsigned)std::min<uint64_t>((work + 255) / 256, 1024);
+        noalloc_check<<<blocks, 256, 0, s>>>(d_rowptr, d_col, n, (uint64_t)nnz, scratch);
+        uint32_t bad = 0;
+        KC_CUDA(cudaGetLastError());
+        KC_CUDA(cudaMemcpyAsync(&bad, reinterpret_cast<uint32_t *>(scratch) + 8, sizeof(bad), cudaMemcpyDeviceToHost,
+                                s));
+        KC_CUDA(cudaStreamSynchronize(s));
+        if (bad)
+            return fail(KC_ERR_INVALID,
+                        "kc_decompose_noalloc: %u row offsets or column ids invalid (ids must be < n = %u, "
+                        "offsets non-decreasing from 0)", bad, n);
+    }
     uint32_t *ctrl = reinterpret_cast<uint32_t *>(scratch);
     BatchArgs A;
     A.rowptr = d_rowptr;
@@ -866,13 +920,9 @@ extern "C" int kc_decompose_noalloc(const int64_t *d_rowptr, const uint32_t *d_c
     A.alist = nullptr;  // scans the vertex range every level: no list storage
     A.alist_stride = 0;
     const size_t smem = ((A.smem_n * sizeof(uint32_t) + 15) & ~size_t(15)) + ((A.smem_n + 31) / 32) * 4 + 16;
-    {
-        // the batch planner sets this kernel's shared-memory limit for its own
-        // launches; restore what this launch needs right before it
-        std::lock_guard<std::mutex> lk(g_noalloc_mu);
-        KC_CUDA(cudaFuncSetAttribute(batch_peel<uint32_t, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        batch_peel<uint32_t, true><<<1, 1024, smem, s>>>(A);
-    }
+    // the kernel's shared-memory limit was raised to the device maximum once,
+    // in noalloc_setup, and is never lowered
+    batch_peel<uint32_t, true><<<1, 1024, smem, s>>>(A);
     KC_CUDA(cudaGetLastError());
     KC_CUDA(cudaStreamSynchronize(s));
     return KC_OK;

@@ -1,6 +1,6 @@
 // Persistent bucket peel: the k-core path of peelone / gppeel / peelone_dyn /
-// peel_dyn (peel/peelone.cu:14-91,157-186; peel/gppeel.cu:12-104,398-440;
-// peel/src/peelone-dyn.cc:2-117,141-158; peel/src/peel-dyn.cc:2-131,323-341)
+// peel_dyn (peel/peelone.cu:14-91,157-186; peel/gppeel.cu:12-104,186-228;
+// peel/src/peelone-dyn.cc:2-117,141-158; peel/src/peel-dyn.cc:2-131,155-171)
 // as ONE cooperative launch per decomposition instead of one host round trip
 // per (sub)level.
 //
@@ -148,7 +148,7 @@ __global__ void peel_ctl_reset(PeelCtl *ctl, unsigned int grid) {
     ctl->kmax = 0;
 }
 
-// Degree-0 vertices get core 1 in GPP mode (gppeel.cu:247-252: its first
+// Degree-0 vertices get core 1 in GPP mode (gppeel.cu:35-39: its first
 // level is 1 and every vertex with residual degree <= level is deleted).
 __global__ void gpp_zero_to_one(const int64_t *__restrict__ rowptr, uint32_t n, uint32_t *core) {
     for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n; v += (uint64_t)gridDim.x * blockDim.x)

@@ -3,7 +3,7 @@
 The reference's ``peel/main.cu`` holds a ``Graph`` loaded from a MatrixMarket
 file (``peel/inc/graph.h:5-21``, loader ``peel/src/graph.cpp:58-133``) and
 times ``int peel_dyn(Graph&)`` / ``int peelone_dyn(Graph&)``
-(``peel/src/peel-dyn.cc:301-350``, ``peel/src/peelone-dyn.cc:120-168``) with
+(``peel/src/peel-dyn.cc:133-182``, ``peel/src/peelone-dyn.cc:120-168``) with
 ``repSimulation`` (``peel/main.cu:28-49``). This module keeps that shape over
 ``libkcore``: the functions take a ``Graph``, run one decomposition on the GPU,
 set ``g.kmax`` and return whole milliseconds. The graph stays resident on the
@@ -87,7 +87,7 @@ def _run(g: Graph, method: str) -> int:
 
 
 def peel_dyn(g: Graph) -> int:
-    """``int peel_dyn(Graph&)`` (``peel/src/peel-dyn.cc:301-350``)."""
+    """``int peel_dyn(Graph&)`` (``peel/src/peel-dyn.cc:133-182``)."""
     return _run(g, "peel_dyn")
 
 
@@ -102,7 +102,7 @@ def peelone(g: Graph) -> int:
 
 
 def gppeel(g: Graph) -> int:
-    """The gppeel driver's timed loop (``peel/gppeel.cu:398-440``); degree-0
+    """The gppeel driver's timed loop (``peel/gppeel.cu:186-228``); degree-0
     vertices report core 1 as the reference's do."""
     return _run(g, "gppeel")
 
