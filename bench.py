@@ -1,11 +1,12 @@
 #!/usr/bin/env python
-"""Benchmark: M edges/s to full k-core decomposition on one GB300.
+"""Benchmark: M edges/s to full k-core on one GB300.
 
-Default workload: one R-MAT graph, scale 22, edge factor 16
-(a, b, c, d = 0.57, 0.19, 0.19, 0.05), de-duplicated and symmetrised
-(4.19M vertices, ~130M directed CSR entries), generated on the device from a
-fixed seed.  A step is one full decomposition of that graph, from the
-device-resident CSR to the core-number array.
+Default workload (the largest single-graph configuration): R-MAT scale 25,
+edge factor 16 (a, b, c, d = 0.57, 0.19, 0.19, 0.05) plus a planted
+4,000-vertex subgraph at edge probability 0.6, de-duplicated and symmetrised
+(33.5M vertices, ~1.06B directed CSR entries, k_max 2,308), generated on the
+device from fixed seeds.  A step is one full decomposition of that graph,
+from the device-resident CSR to the core-number array.
 
 Printed JSON line (rank 0):
   value      undirected edges x steps x ranks / max-over-ranks device time
@@ -19,13 +20,16 @@ Printed JSON line (rank 0):
              main kernel's average CUDA-event duration, against the measured
              HBM copy bandwidth;
   cpu_baseline  serial Batagelj-Zaversnik (the oracle) on the same graph, on
-             one host core;
-  batched / serving / inputs  the 4096-graph batched form against the plain
-             form, the request server's latency, and the input/output paths
-             (generation, edge files, MatrixMarket parse, snapshots, k-core
-             extraction).
+             one host core, median of 3 runs;
+  rmat22 / batched / serving / inputs  R-MAT scale 22 (the reference-sized
+             graph) timed the same way, the 4096-graph batched form against
+             the plain form, the request server's latency, and the
+             input/output paths (generation, edge files, MatrixMarket parse,
+             snapshots, k-core extraction).
 `--impl reference` times the reference's CPU path (serial Batagelj-Zaversnik,
-the oracle port) on the host cores on the same graph, generated on the host.
+the oracle port) on the host cores on the same graph, generated on the host:
+each step is one full decomposition, and the steps run as independent serial
+decompositions on all host threads (throughput of the host).
 `--gpus N` (under torchrun) runs N independent replicas: the decomposition of
 one graph does not shard, every rank decomposes its own copy.
 """
@@ -173,7 +177,7 @@ def make_graph(pg, wl, device):
     return pg.rmat_planted_graph(wl["scale"], wl["ef"], wl["k"], wl["p"], wl["seed"], device=device)
 
 
-def host_graph(wl):
+def host_graph(wl, threads=1):
     """The same graph built on the host only (numpy + the oracle), for the CPU arm."""
     import numpy as np
 
@@ -181,16 +185,17 @@ def host_graph(wl):
     from oracle import gen
     if wl["kind"] == "rmat":
         n = 1 << wl["scale"]
-        s, d = gen.rmat(wl["scale"], wl["ef"] * n, wl["seed"])
+        s, d = gen.rmat(wl["scale"], wl["ef"] * n, wl["seed"], threads=threads)
     elif wl["kind"] == "er":
         n = wl["n"]
         s, d = gen.er(wl["n"], wl["m"], wl["seed"])
     else:
         n = 1 << wl["scale"]
-        s1, d1 = gen.rmat(wl["scale"], wl["ef"] * n, wl["seed"])
+        s1, d1 = gen.rmat(wl["scale"], wl["ef"] * n, wl["seed"], threads=threads)
         s2, d2 = gen.planted(n, wl["k"], wl["p"], wl["seed"] + 1)
         s, d = np.concatenate([s1, s2]), np.concatenate([d1, d2])
-    return oracle.csr_dedup(n, s, d)
+        del s1, d1
+    return oracle.csr_dedup(n, s, d, threads=threads)
 
 
 def cpu_bz(rowptr, col, reps):
@@ -204,15 +209,32 @@ def cpu_bz(rowptr, col, reps):
 
 
 def run_reference(args, wl, world, rank, dist):
-    """The reference's CPU path (serial Batagelj-Zaversnik port) on host cores."""
+    """The reference's CPU path (serial Batagelj-Zaversnik port) on host cores:
+    every step is one full decomposition of the workload graph; the steps run
+    as independent serial decompositions on all host threads (the oracle
+    releases the interpreter lock), so the value is the host's throughput."""
     if rank != 0:
         return 0
-    rowptr, col = host_graph(wl)
+    import oracle
+    threads = max(1, os.cpu_count() or 1)
+    t0 = time.perf_counter()
+    rowptr, col = host_graph(wl, threads=threads)
+    build_s = time.perf_counter() - t0
     n = rowptr.size - 1
     m = int(rowptr[-1]) // 2
-    times = cpu_bz(rowptr, col, args.warmup + args.steps)[args.warmup:]
-    total = sum(times)
+    workers = max(1, min(threads, args.steps))
+
+    def one(_i):
+        oracle.bz(rowptr, col)
+
+    with ThreadPoolExecutor(workers) as ex:
+        list(ex.map(one, range(args.warmup)))
+        t0 = time.perf_counter()
+        list(ex.map(one, range(args.steps)))
+        total = time.perf_counter() - t0
     value = m * args.steps / total / 1e6
+    sample = ("full graph, %d decompositions as independent serial Batagelj-Zaversnik runs on %d host threads "
+              "(%d warm-up runs first)" % (args.steps, workers, args.warmup))
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "M edges/s", "impl": "reference",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -220,10 +242,10 @@ def run_reference(args, wl, world, rank, dist):
         "vs_baseline": None, "dtype": "u32", "data": "synthetic",
         "config": {"workload": wl["desc"], "n": n, "m_undirected": m, "nnz": int(rowptr[-1]),
                    "method": "serial Batagelj-Zaversnik (oracle port), host", "l2": "n/a (host)"},
-        "cpu_baseline": {"value": round(value, 3), "unit": "M edges/s", "cores": 1, "kind": "port",
-                         "sample": "full graph, %d decompositions" % args.steps},
+        "cpu_baseline": {"value": round(value, 3), "unit": "M edges/s", "cores": workers, "kind": "port",
+                         "sample": sample},
         "e2e": {"value": round(value, 3), "unit": "M edges/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "host": {"nproc": os.cpu_count(), "cpu": _cpu_model()},
+        "host": {"nproc": os.cpu_count(), "cpu": _cpu_model(), "graph_build_s": round(build_s, 2)},
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -315,11 +337,12 @@ def run_engine(args, wl, world, rank, local, dist):
 
     rowptr, col = g.csr()
     if rank == 0 and world == 1 and not args.no_cpu:
-        reps = 1
+        reps = 3
         t = cpu_bz(rowptr, col, reps)
         line["cpu_baseline"] = {"value": round(m / statistics.median(t) / 1e6, 3), "unit": "M edges/s",
                                 "cores": 1, "kind": "port",
-                                "sample": "full graph, serial Batagelj-Zaversnik, %d run(s), %.2f s" % (reps, t[0]),
+                                "sample": "full graph, serial Batagelj-Zaversnik, median of %d runs (%s s)"
+                                          % (reps, ", ".join("%.2f" % x for x in t)),
                                 "host": _cpu_model(), "nproc": os.cpu_count()}
 
     # end to end through the C ABI with pinned host buffers
@@ -397,14 +420,64 @@ def run_engine(args, wl, world, rank, local, dist):
             line["serving"] = serve_section(pg, device, args.serve_requests, args.serve_rate)
         except Exception as e:  # noqa: BLE001
             line["serving"] = {"error": "%s: %s" % (type(e).__name__, e)}
+    del rowptr, col
+    c2 = None
+    if world == 1 and args.workload != "rmat22" and not args.no_c2:
+        try:
+            line["rmat22"], c2 = graph_section(pg, device, sptr, "rmat22", method, args.steps)
+        except Exception as e:  # noqa: BLE001
+            line["rmat22"] = {"error": "%s: %s" % (type(e).__name__, e)}
     if world == 1 and not args.no_inputs:
         try:
-            line["inputs"] = inputs_section(pg, device, wl, rowptr, col, st.kmax)
+            if c2 is None:
+                gi = make_graph(pg, WORKLOADS["rmat22"], device)
+                c2 = gi.csr() + (gi.decompose_device(method, stats=True).kmax,)
+                gi.free()
+            line["inputs"] = inputs_section(pg, device, WORKLOADS["rmat22"], *c2)
         except Exception as e:  # noqa: BLE001
             line["inputs"] = {"error": "%s: %s" % (type(e).__name__, e)}
     if rank == 0:
         print(json.dumps(line), flush=True)
     return 0
+
+
+def graph_section(pg, device, sptr, name, method, steps):
+    """One more single-graph workload timed like the headline (CUDA events
+    around `steps` decompositions after warm-up, the main kernel's own
+    events for the roofline); returns the section and (rowptr, col, kmax)."""
+    import torch
+    wl = WORKLOADS[name]
+    g = make_graph(pg, wl, device)
+    n, nnz = g.n, g.nnz
+    for _ in range(3):
+        g.decompose_device(method, stream=sptr)
+    stream = torch.cuda.ExternalStream(sptr, device=device)
+    torch.cuda.synchronize(device)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    kernel_ms = []
+    ev0.record(stream)
+    for _ in range(steps):
+        g.decompose_device(method, stream=sptr)
+        kernel_ms.append(g.last_timing()[1])
+    ev1.record(stream)
+    torch.cuda.synchronize(device)
+    ms = ev0.elapsed_time(ev1) / steps
+    st = g.decompose_device(method, stream=sptr, stats=True)
+    kavg = statistics.mean(kernel_ms)
+    bytes_alg = 10 * nnz + 16 * n + 8
+    peak, peak_kind = load_peaks()
+    kernel_name = "hindex_kernel" if pg.method_id(method) in (0, 1, 2) else "peel_kernel"
+    out = {"workload": wl["desc"], "n": n, "nnz": nnz, "m_undirected": nnz // 2, "method": method,
+           "steps": steps, "ms_per_step": round(ms, 4), "value": round((nnz // 2) / (ms / 1e3) / 1e6, 3),
+           "unit": "M edges/s", "kmax": st.kmax, "levels": st.levels, "level_indices": st.iterations,
+           "roofline": {"kernel": kernel_name, "kernel_ms_avg": round(kavg, 4), "bytes_per_launch": bytes_alg,
+                        "achieved": round(bytes_alg / (kavg / 1e3) / 1e9, 1), "peak": peak, "peak_kind": peak_kind,
+                        "frac": round(bytes_alg / (kavg / 1e3) / 1e9 / peak, 4),
+                        "traffic": load_traffic(kernel_name, name)}}
+    rowptr, col = g.csr()
+    g.free()
+    return out, (rowptr, col, st.kmax)
 
 
 def inputs_section(pg, device, wl, rowptr, col, kmax):
@@ -635,7 +708,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["engine", "reference"], default="engine")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="rmat22")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="rmat25planted")
     ap.add_argument("--method", default="peelone_dyn")
     ap.add_argument("--clock-window", type=float, default=1.5,
                     help="seconds of identical load before the timed steps, so clocks are sampled under load")
@@ -643,6 +716,7 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the 4096-graph batched-vs-plain section")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving section")
     ap.add_argument("--no-inputs", action="store_true", help="skip the input/output path section")
+    ap.add_argument("--no-c2", action="store_true", help="skip the R-MAT scale 22 section")
     ap.add_argument("--batch-graphs", type=int, default=4096, help="graphs in the batched section")
     ap.add_argument("--no-autotune", action="store_true", help="batched section: keep the default configuration")
     ap.add_argument("--serve-requests", type=int, default=40)

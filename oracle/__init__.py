@@ -40,7 +40,7 @@ def build(force: bool = False) -> str:
             and os.path.getmtime(LIB_PATH) >= os.path.getmtime(_SRC)):
         return LIB_PATH
     tmp = LIB_PATH + ".tmp%d" % os.getpid()
-    subprocess.check_call(["gcc", "-O2", "-std=c11", "-shared", "-fPIC", _SRC, "-o", tmp])
+    subprocess.check_call(["gcc", "-O2", "-std=gnu11", "-pthread", "-shared", "-fPIC", _SRC, "-o", tmp])
     os.replace(tmp, LIB_PATH)
     return LIB_PATH
 
@@ -73,6 +73,11 @@ def lib():
             L.orc_csr_dedup.restype = ctypes.c_int64
             L.orc_check_local.argtypes = [ctypes.c_uint32, i64p, u32p, u32p]
             L.orc_check_local.restype = ctypes.c_uint64
+            L.orc_csr_dedup_mt.argtypes = [ctypes.c_uint32, ctypes.c_uint64, u32p, u32p, i64p, u32p, ctypes.c_int]
+            L.orc_csr_dedup_mt.restype = ctypes.c_int64
+            L.orc_gen_rmat_mt.argtypes = [ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64,
+                                          ctypes.c_uint64, ctypes.c_uint64, u32p, u32p, ctypes.c_int]
+            L.orc_gen_rmat_mt.restype = None
             _lib = L
     return _lib
 
@@ -177,17 +182,22 @@ def make_ugraph(n, src, dst, part_size=64):
     return node_ptr[:n], edge_list[:2 * m + n], parts[:2 * k].reshape(k, 2)
 
 
-def csr_dedup(n, src, dst):
-    """Sorted de-duplicated CSR (rowptr int64[n+1], col uint32[nnz]) of an edge list."""
+def csr_dedup(n, src, dst, threads=1):
+    """Sorted de-duplicated CSR (rowptr int64[n+1], col uint32[nnz]) of an
+    edge list; threads > 1 builds it on that many host threads (same result)."""
     src = np.ascontiguousarray(src, dtype=np.uint32)
     dst = np.ascontiguousarray(dst, dtype=np.uint32)
     m = src.size
     rowptr = np.zeros(n + 1, dtype=np.int64)
-    col = np.zeros(max(2 * m, 1), dtype=np.uint32)
+    col = np.empty(max(2 * m, 1), dtype=np.uint32)
     s = src if m else np.zeros(1, np.uint32)
     d = dst if m else np.zeros(1, np.uint32)
-    k = lib().orc_csr_dedup(n, m, _p(s, ctypes.c_uint32), _p(d, ctypes.c_uint32),
-                            _p(rowptr, ctypes.c_int64), _p(col, ctypes.c_uint32))
+    if threads > 1:
+        k = lib().orc_csr_dedup_mt(n, m, _p(s, ctypes.c_uint32), _p(d, ctypes.c_uint32),
+                                   _p(rowptr, ctypes.c_int64), _p(col, ctypes.c_uint32), int(threads))
+    else:
+        k = lib().orc_csr_dedup(n, m, _p(s, ctypes.c_uint32), _p(d, ctypes.c_uint32),
+                                _p(rowptr, ctypes.c_int64), _p(col, ctypes.c_uint32))
     if k < 0:
         raise MemoryError("orc_csr_dedup")
     return rowptr, col[:k]

@@ -19,8 +19,9 @@ def _thr(p):
     return min(max(int(np.floor(p * 4294967296.0)), 0), 4294967296)
 
 
-def rmat(scale, m, seed, a=0.57, b=0.19, c=0.19):
-    """R-MAT edge list (src, dst); the C restatement for large m."""
+def rmat(scale, m, seed, a=0.57, b=0.19, c=0.19, threads=1):
+    """R-MAT edge list (src, dst); the C restatement for large m (on
+    `threads` host threads when threads > 1)."""
     if m > 1 << 20:
         import ctypes
         import oracle
@@ -31,8 +32,12 @@ def rmat(scale, m, seed, a=0.57, b=0.19, c=0.19):
         L.orc_gen_rmat.restype = None
         src = np.empty(m, dtype=np.uint32)
         dst = np.empty(m, dtype=np.uint32)
-        L.orc_gen_rmat(scale, m, _thr(a), _thr(a + b), _thr(a + b + c), seed,
-                       src.ctypes.data_as(u32p), dst.ctypes.data_as(u32p))
+        if threads > 1:
+            L.orc_gen_rmat_mt(scale, m, _thr(a), _thr(a + b), _thr(a + b + c), seed,
+                              src.ctypes.data_as(u32p), dst.ctypes.data_as(u32p), int(threads))
+        else:
+            L.orc_gen_rmat(scale, m, _thr(a), _thr(a + b), _thr(a + b + c), seed,
+                           src.ctypes.data_as(u32p), dst.ctypes.data_as(u32p))
         return src, dst
     return rmat_numpy(scale, m, seed, a, b, c)
 

@@ -28,6 +28,9 @@
  *   orc_csr_dedup     sorted, de-duplicated CSR restating
  *                     peel/src/graph.cpp:103-131.
  *   orc_check_local   per-vertex fixpoint test of a core vector.
+ *   orc_gen_rmat_mt / orc_csr_dedup_mt  the host R-MAT generator and the
+ *                     de-duplicating CSR build on several threads (the
+ *                     CPU arm of the benchmark builds billion-entry graphs).
  *
  * Parity is pinned by the reference's own known answer (example.txt: every
  * core is 2) and by golden files produced with the reference's own loader and
@@ -39,6 +42,7 @@
  * every undirected edge present, no self-loops.  Parallel entries (the
  * reference's COO loader keeps duplicate lines) count with multiplicity.
  */
+#include <pthread.h>
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
@@ -433,4 +437,167 @@ void orc_gen_rmat(uint32_t scale, uint64_t m, uint64_t ta, uint64_t tab, uint64_
         src[i] = u;
         dst[i] = v;
     }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Multi-threaded forms of the two host builders above, for graphs of a
+ * billion entries (R-MAT scale 25: the serial forms take minutes).  Same
+ * output bit for bit: the generator is counter-based, and every CSR row is
+ * sorted and made unique after its entries are placed, so the order in which
+ * threads place them does not matter.                                      */
+
+typedef void (*orc_range_fn)(void *ctx, uint64_t lo, uint64_t hi);
+typedef struct { orc_range_fn fn; void *ctx; uint64_t lo, hi; } orc_job;
+
+static void *orc_job_run(void *p)
+{
+    orc_job *j = (orc_job *)p;
+    j->fn(j->ctx, j->lo, j->hi);
+    return NULL;
+}
+
+/* Runs fn over [0, total) split into `threads` contiguous ranges. */
+static void orc_parallel(int threads, uint64_t total, orc_range_fn fn, void *ctx)
+{
+    enum { MAXT = 128 };
+    pthread_t th[MAXT];
+    orc_job jobs[MAXT];
+    int started[MAXT];
+    if (threads < 1) threads = 1;
+    if (threads > MAXT) threads = MAXT;
+    for (int t = 0; t < threads; t++) {
+        jobs[t].fn = fn;
+        jobs[t].ctx = ctx;
+        jobs[t].lo = total * (uint64_t)t / (uint64_t)threads;
+        jobs[t].hi = total * (uint64_t)(t + 1) / (uint64_t)threads;
+        started[t] = t > 0 && pthread_create(&th[t], NULL, orc_job_run, &jobs[t]) == 0;
+    }
+    orc_job_run(&jobs[0]);
+    for (int t = 1; t < threads; t++) {
+        if (started[t]) pthread_join(th[t], NULL);
+        else orc_job_run(&jobs[t]);
+    }
+}
+
+typedef struct {
+    uint32_t scale;
+    uint64_t ta, tab, tabc, seed;
+    uint32_t *src, *dst;
+} orc_rmat_ctx;
+
+static void orc_rmat_range(void *p, uint64_t lo, uint64_t hi)
+{
+    orc_rmat_ctx *c = (orc_rmat_ctx *)p;
+    for (uint64_t i = lo; i < hi; i++) {
+        uint64_t base = orc_mix64(c->seed * 0xD1B54A32D192ED03ull + i);
+        uint32_t u = 0, v = 0;
+        uint64_t word = 0;
+        for (uint32_t b = 0; b < c->scale; b++) {
+            if ((b & 1) == 0) word = orc_mix64(base ^ ((uint64_t)((b >> 1) + 1) * 0xA24BAED4963EE407ull));
+            uint32_t r = (uint32_t)(word >> (32 * (b & 1)));
+            uint32_t q = r < c->ta ? 0u : (r < c->tab ? 1u : (r < c->tabc ? 2u : 3u));
+            u = (u << 1) | (q >> 1);
+            v = (v << 1) | (q & 1u);
+        }
+        c->src[i] = u;
+        c->dst[i] = v;
+    }
+}
+
+/* orc_gen_rmat on `threads` threads. */
+void orc_gen_rmat_mt(uint32_t scale, uint64_t m, uint64_t ta, uint64_t tab, uint64_t tabc, uint64_t seed,
+                     uint32_t *src, uint32_t *dst, int threads)
+{
+    orc_rmat_ctx c = {scale, ta, tab, tabc, seed, src, dst};
+    orc_parallel(threads, m, orc_rmat_range, &c);
+}
+
+typedef struct {
+    uint64_t m;
+    const uint32_t *src, *dst;
+    int64_t *cnt;     /* row sizes, then row fill cursors */
+    uint32_t *col;    /* scatter target */
+    uint32_t *ulen;   /* unique entries per row */
+    const int64_t *start;
+} orc_csr_ctx;
+
+static void orc_csr_count(void *p, uint64_t lo, uint64_t hi)
+{
+    orc_csr_ctx *c = (orc_csr_ctx *)p;
+    for (uint64_t i = lo; i < hi; i++) {
+        if (c->src[i] == c->dst[i]) continue;
+        __atomic_fetch_add(&c->cnt[c->src[i]], 1, __ATOMIC_RELAXED);
+        __atomic_fetch_add(&c->cnt[c->dst[i]], 1, __ATOMIC_RELAXED);
+    }
+}
+
+static void orc_csr_scatter(void *p, uint64_t lo, uint64_t hi)
+{
+    orc_csr_ctx *c = (orc_csr_ctx *)p;
+    for (uint64_t i = lo; i < hi; i++) {
+        uint32_t s = c->src[i], d = c->dst[i];
+        if (s == d) continue;
+        c->col[__atomic_fetch_add(&c->cnt[s], 1, __ATOMIC_RELAXED)] = d;
+        c->col[__atomic_fetch_add(&c->cnt[d], 1, __ATOMIC_RELAXED)] = s;
+    }
+}
+
+static void orc_csr_rows(void *p, uint64_t lo, uint64_t hi)
+{
+    orc_csr_ctx *c = (orc_csr_ctx *)p;
+    uint64_t maxlen = 0;
+    for (uint64_t v = lo; v < hi; v++) {
+        uint64_t l = (uint64_t)(c->start[v + 1] - c->start[v]);
+        if (l > maxlen) maxlen = l;
+    }
+    uint32_t *tmp = maxlen > 32 ? (uint32_t *)malloc((size_t)maxlen * sizeof(uint32_t)) : NULL;
+    for (uint64_t v = lo; v < hi; v++) {
+        uint32_t *row = c->col + c->start[v];
+        uint64_t l = (uint64_t)(c->start[v + 1] - c->start[v]);
+        if (l > 32 && tmp) {
+            radix_u32(row, tmp, l);
+        } else {
+            for (uint64_t a = 1; a < l; a++) {  /* insertion sort of a short row */
+                uint32_t x = row[a];
+                uint64_t b = a;
+                while (b > 0 && row[b - 1] > x) { row[b] = row[b - 1]; b--; }
+                row[b] = x;
+            }
+        }
+        uint64_t w = 0;
+        for (uint64_t j = 0; j < l; j++)
+            if (j == 0 || row[j] != row[j - 1]) row[w++] = row[j];
+        c->ulen[v] = (uint32_t)w;
+    }
+    free(tmp);
+}
+
+/* orc_csr_dedup on `threads` threads (same arguments and result). */
+int64_t orc_csr_dedup_mt(uint32_t n, uint64_t m, const uint32_t *src, const uint32_t *dst,
+                         int64_t *rowptr, uint32_t *col, int threads)
+{
+    int64_t *start = (int64_t *)calloc((size_t)n + 2, sizeof(int64_t));
+    uint32_t *ulen = (uint32_t *)malloc(((size_t)n + 1) * sizeof(uint32_t));
+    if (!start || !ulen) { free(start); free(ulen); return -1; }
+    orc_csr_ctx c = {m, src, dst, start + 1, col, ulen, start};
+    orc_parallel(threads, m, orc_csr_count, &c);
+    for (uint32_t v = 0; v < n; v++) start[v + 1] += start[v];
+    int64_t *fill = (int64_t *)malloc(((size_t)n + 1) * sizeof(int64_t));
+    if (!fill) { free(start); free(ulen); return -1; }
+    memcpy(fill, start, ((size_t)n + 1) * sizeof(int64_t));
+    c.cnt = fill;
+    orc_parallel(threads, m, orc_csr_scatter, &c);
+    free(fill);
+    orc_parallel(threads, n, orc_csr_rows, &c);
+    /* compaction: rows move down (never up), in increasing row order */
+    int64_t w = 0;
+    rowptr[0] = 0;
+    for (uint32_t v = 0; v < n; v++) {
+        if (w != start[v]) memmove(col + w, col + start[v], (size_t)ulen[v] * sizeof(uint32_t));
+        w += ulen[v];
+        rowptr[v + 1] = w;
+    }
+    free(start);
+    free(ulen);
+    return w;
 }

@@ -128,3 +128,19 @@ def test_rmat_restatements_agree():
     s1, d1 = gen.rmat_numpy(16, 5000, 9)
     s2, d2 = gen.rmat(16, (1 << 20) + 7, 9)
     assert np.array_equal(s1, s2[:5000]) and np.array_equal(d1, d2[:5000])
+
+
+def test_threaded_host_builders_equal_serial():
+    """The multi-threaded R-MAT generator and CSR build (used to build the
+    billion-entry graphs of the CPU benchmark arm) give exactly the serial
+    results, including rows long enough for the radix path and self-loops."""
+    from oracle import gen
+    s1, d1 = gen.rmat(16, (1 << 20) + 12345, 7)
+    s4, d4 = gen.rmat(16, (1 << 20) + 12345, 7, threads=4)
+    assert np.array_equal(s1, s4) and np.array_equal(d1, d4)
+    rp1, c1 = oracle.csr_dedup(1 << 16, s1, d1)
+    for t in (2, 5):
+        rp, c = oracle.csr_dedup(1 << 16, s1, d1, threads=t)
+        assert np.array_equal(rp, rp1) and np.array_equal(c, c1)
+    rp0, c0 = oracle.csr_dedup(5, np.array([], np.uint32), np.array([], np.uint32), threads=3)
+    assert rp0.tolist() == [0] * 6 and c0.size == 0
