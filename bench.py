@@ -645,11 +645,10 @@ def serve_section(pg, device, requests, rate_hz, sweep_rates=(10.0, 50.0, 200.0)
 
     from pico_gb300 import workloads
     base = pg.rmat_graph(22, 16, 2, device=device)
-    rp, col = base.csr()
+    rp_base, col_base = base.csr()
     t_gen = time.perf_counter()
-    reqs = workloads.serve_stream(rp, col, requests, seed=5, rate_hz=rate_hz, device=device)
+    reqs = workloads.serve_stream(rp_base, col_base, requests, seed=5, rate_hz=rate_hz, device=device)
     gen_s = time.perf_counter() - t_gen
-    del rp, col
     srv = pg.Server(base, decompose_slots=2, max_batch_graphs=64)
     t0 = time.perf_counter()
     res = workloads.run_stream(srv, reqs, realtime=True)
@@ -676,6 +675,8 @@ def serve_section(pg, device, requests, rate_hz, sweep_rates=(10.0, 50.0, 200.0)
                       "p99_ms": round(float(np.percentile(l2, 99)), 3),
                       "throughput_req_s": round(len(res2) / w2, 2), "max_inflight": int(st2["max_inflight"]),
                       "failed": int(st2["failed"])})
+    exact, checked = serve_exact(rp_base, col_base, reqs, res)
+    del rp_base, col_base
     upd = [r for q, r in zip(reqs, res) if q["kind"] == "update"]
     dec = [r for q, r in zip(reqs, res) if q["kind"] == "decompose"]
     upd_edges = sum(q["ins"][0].size + q["dels"][0].size for q in reqs if q["kind"] == "update")
@@ -698,8 +699,62 @@ def serve_section(pg, device, requests, rate_hz, sweep_rates=(10.0, 50.0, 200.0)
         "throughput_m_edges_s": round((upd_edges + dec_edges) / wall / 1e6, 3),
         "failed": int(st["failed"]), "decompose_launches": int(st["decompose_launches"]),
         "max_inflight": int(st["max_inflight"]), "latency": "submission (arrival) to result on host",
+        "exact": exact, "exact_checked": checked,
         "generate_s": round(gen_s, 2), "rate_sweep": sweep,
     }
+
+
+def core_digest(core):
+    """The request server's digest of a core array: sum of core[v] *
+    splitmix64(v + 1), mod 2^64."""
+    import numpy as np
+
+    from oracle import gen
+    v = np.arange(1, core.size + 1, dtype=np.uint64)
+    with np.errstate(over="ignore"):
+        return int((core.astype(np.uint64) * gen.mix64(v)).sum(dtype=np.uint64))
+
+
+def serve_exact(base_rowptr, base_col, reqs, results):
+    """Checks every served result against Batagelj-Zaversnik on the host,
+    outside the timed latencies: decompositions on their own graphs, and each
+    update on the resident graph as it stood after that update (the edge set
+    replayed on the host: deletions, then insertions).  Compares the
+    server's digests of the core arrays.  Returns (all equal, count)."""
+    import numpy as np
+
+    import oracle
+    from pico_gb300 import workloads
+    keys = workloads.edge_keys(base_rowptr, base_col)
+    n = base_rowptr.size - 1
+    jobs = []
+    for q, r in zip(reqs, results):
+        if q["kind"] == "decompose":
+            jobs.append((q["rowptr"], q["col"], None, r["digest"]))
+            continue
+        (is_, id_), (ds_, dd_) = q["ins"], q["dels"]
+        dk = np.minimum(ds_, dd_).astype(np.uint64) << np.uint64(32) | np.maximum(ds_, dd_).astype(np.uint64)
+        ik = np.minimum(is_, id_).astype(np.uint64) << np.uint64(32) | np.maximum(is_, id_).astype(np.uint64)
+        p = np.searchsorted(keys, dk)
+        hit = (p < keys.size) & (keys[np.minimum(p, keys.size - 1)] == dk)
+        keys = np.delete(keys, p[hit])
+        ik = np.unique(ik[is_ != id_])
+        p = np.searchsorted(keys, ik)
+        ik = ik[~((p < keys.size) & (keys[np.minimum(p, keys.size - 1)] == ik))]
+        keys = np.insert(keys, np.searchsorted(keys, ik), ik)
+        jobs.append((None, None, keys, r["digest"]))
+
+    def check(job):
+        rp, col, k, want = job
+        if k is not None:
+            rp, col = oracle.csr_dedup(n, (k >> np.uint64(32)).astype(np.uint32),
+                                       (k & np.uint64(0xffffffff)).astype(np.uint32), threads=2)
+        core, _ = oracle.bz(rp, col)
+        return core_digest(core) == want
+
+    with ThreadPoolExecutor(max(1, min(8, (os.cpu_count() or 2) // 2))) as ex:
+        ok = list(ex.map(check, jobs))
+    return all(ok), len(ok)
 
 
 def main():

@@ -27,3 +27,36 @@ def test_reference_arm_prints_one_contract_line():
     assert cb["value"] == d["value"] and cb["cores"] >= 1 and cb["kind"] in ("port", "reference") and cb["sample"]
     e = d["e2e"]
     assert e["value"] == d["value"] and e["h2d_bytes_per_step"] == 0 and e["d2h_bytes_per_step"] == 0
+
+
+def test_serving_exactness_replay_detects_a_wrong_result():
+    """bench.serve_exact replays the update stream on the host edge set and
+    compares each served digest with Batagelj-Zaversnik; one wrong digest
+    makes the whole check fail."""
+    import numpy as np
+
+    import oracle
+    sys.path.insert(0, ROOT)
+    import bench
+    from pico_gb300 import workloads
+    rng = np.random.default_rng(1)
+    n = 2000
+    rp, col = oracle.csr_dedup(n, rng.integers(0, n, 20000).astype(np.uint32),
+                               rng.integers(0, n, 20000).astype(np.uint32))
+    cur = workloads.edge_keys(rp, col)
+    split = lambda k: ((k >> np.uint64(32)).astype(np.uint32), (k & np.uint64(0xffffffff)).astype(np.uint32))
+    reqs, res = [], []
+    for _ in range(3):
+        dk = rng.choice(cur, 50, replace=False)
+        a = rng.integers(0, n, 60).astype(np.uint64)
+        b = rng.integers(0, n, 60).astype(np.uint64)
+        ik = (np.minimum(a, b) << np.uint64(32)) | np.maximum(a, b)
+        reqs.append(dict(kind="update", ins=split(ik), dels=split(dk)))
+        cur = np.union1d(np.setdiff1d(cur, dk), ik[a != b])
+        r2, c2 = oracle.csr_dedup(n, *split(cur))
+        res.append(dict(digest=bench.core_digest(oracle.bz(r2, c2)[0])))
+    reqs.append(dict(kind="decompose", rowptr=rp, col=col))
+    res.append(dict(digest=bench.core_digest(oracle.bz(rp, col)[0])))
+    assert bench.serve_exact(rp, col, reqs, res) == (True, 4)
+    res[1]["digest"] += 1
+    assert bench.serve_exact(rp, col, reqs, res) == (False, 4)

@@ -93,3 +93,76 @@ def test_update_rejects_bad_ids_and_multigraphs():
     with pytest.raises(pg.KCoreError) as e:
         h.update(([0], [2]), None)
     assert e.value.code == pg.KC_ERR_UNSUPPORTED
+
+
+def c5_batch(rng, keys, n, size):
+    """One edge-update batch of the dynamic-serving configuration: `size`
+    edges, half insertions (uniform vertex pairs that are neither self-loops
+    nor current edges) and half deletions (drawn uniformly, without
+    replacement, from the current edge set)."""
+    ni = size // 2
+    nd = size - ni
+    dpos = np.unique(rng.integers(0, keys.size, size=2 * nd))
+    rng.shuffle(dpos)
+    dk = keys[dpos[:nd]]
+    ins = np.zeros(0, np.uint64)
+    while ins.size < ni:
+        a = rng.integers(0, n, size=2 * ni, dtype=np.uint64)
+        b = rng.integers(0, n, size=2 * ni, dtype=np.uint64)
+        k = (np.minimum(a, b) << np.uint64(32)) | np.maximum(a, b)
+        k = k[a != b]
+        p = np.searchsorted(keys, k)
+        k = k[~((p < keys.size) & (keys[np.minimum(p, keys.size - 1)] == k))]
+        ins = np.unique(np.concatenate([ins, k]))
+    ins = rng.permutation(ins)[:ni]
+    split = lambda kk: ((kk >> np.uint64(32)).astype(np.uint32), (kk & np.uint64(0xffffffff)).astype(np.uint32))
+    return split(ins), split(dk), ins, dk
+
+
+def row_keys(rp, col):
+    """Keys (u << 32 | v, u < v) of a CSR with sorted rows, in row order."""
+    n = rp.size - 1
+    src = np.repeat(np.arange(n, dtype=np.uint64), np.diff(rp))
+    m = src < col
+    return (src[m] << np.uint64(32)) | col[m].astype(np.uint64)
+
+
+@pytest.mark.parametrize("mode", ["default", "incremental"])
+def test_c5_rmat22_update_batches_exact(mode):
+    """The dynamic-serving configuration: an R-MAT scale-22 base graph
+    (edge factor 16, seed 2) receives update batches of floor(10^U(3,6))
+    edges, 50/50 insert/delete.  After every batch the CSR holds exactly the
+    expected edge set and the core numbers equal Batagelj-Zaversnik on the
+    updated graph.  "incremental" raises update.incremental_max so that
+    batches of 10^3-10^4 edges take the incremental path."""
+    rng = np.random.default_rng(55 if mode == "default" else 56)
+    g = pg.rmat_graph(22, 16, 2)
+    n = g.n
+    if mode == "incremental":
+        g.set_param("update.incremental_max", 20000)
+        sizes = np.floor(10.0 ** rng.uniform(3.0, 4.0, 4)).astype(np.int64)
+    else:
+        sizes = np.floor(10.0 ** rng.uniform(3.0, 6.0, 5)).astype(np.int64)
+    g.decompose("peelone_dyn")
+    rp, col = g.csr()
+    keys = row_keys(rp, col)
+    for step, size in enumerate(sizes):
+        ins, dels, ik, dk = c5_batch(rng, keys, n, int(size))
+        core, st = g.update(ins, dels)
+        assert st["inserted"] == ik.size and st["deleted"] == dk.size, (step, st)
+        # default threshold (512 edges): every batch of 10^3 or more edges is a
+        # rewrite plus a full decomposition
+        assert st["recomputed"] == (0 if mode == "incremental" else 1), (step, size, st)
+        rp, col = g.csr()
+        new_keys = row_keys(rp, col)
+        assert (new_keys[1:] > new_keys[:-1]).all()  # rows sorted, no repeated neighbours
+        assert new_keys.size == keys.size + ik.size - dk.size
+        p = np.searchsorted(new_keys, ik)
+        assert (new_keys[np.minimum(p, new_keys.size - 1)] == ik).all()
+        p = np.searchsorted(new_keys, dk)
+        assert not ((p < new_keys.size) & (new_keys[np.minimum(p, new_keys.size - 1)] == dk)).any()
+        want, _ = oracle.bz(rp, col)
+        bad = np.flatnonzero(core != want)
+        assert bad.size == 0, (step, int(size), bad.size, st)
+        keys = new_keys
+    g.free()
