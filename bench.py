@@ -427,6 +427,11 @@ def run_engine(args, wl, world, rank, local, dist):
             line["rmat22"], c2 = graph_section(pg, device, sptr, "rmat22", method, args.steps)
         except Exception as e:  # noqa: BLE001
             line["rmat22"] = {"error": "%s: %s" % (type(e).__name__, e)}
+    if world == 1 and not args.no_refgpu:
+        try:
+            line["reference_gpu"] = reference_gpu_section(pg, device, args.refgpu_graphs.split(","))
+        except Exception as e:  # noqa: BLE001
+            line["reference_gpu"] = {"error": "%s: %s" % (type(e).__name__, e)}
     if world == 1 and not args.no_inputs:
         try:
             if c2 is None:
@@ -439,6 +444,76 @@ def run_engine(args, wl, world, rank, local, dist):
     if rank == 0:
         print(json.dumps(line), flush=True)
     return 0
+
+
+REFGPU_GRAPHS = {"er65536": ("Erdos-Renyi G(65536, 1048576), seed 1", "er65536"),
+                 "rmat22": ("R-MAT scale 22, edge factor 16, seed 2", "rmat22")}
+
+
+def reference_gpu_section(pg, device, graphs):
+    """The reference's own GPU drivers (compiled for sm_103a from their
+    sources, run as separate processes on a MatrixMarket file) beside this
+    engine's decomposition of the same file with the same loader semantics:
+    each driver's own printed time (index2core / peelone / gppeel: wall ms of
+    the iteration loop; peel_dyn / peelone_dyn: integer ms of one call)
+    against the CUDA-event time of this engine's decomposition (median of 5),
+    and whether the core arrays are identical.  The peel/src drivers keep
+    fixed per-block queues of 10^6 entries with a device assert on overflow,
+    so they run only on graphs of fewer than 10^6 vertices."""
+    import tempfile
+
+    import numpy as np
+
+    from oracle import ref_gpu
+    if not ref_gpu.sources_present():
+        return {"unavailable": "reference GPU driver sources not copied next to the tree"}
+    t0 = time.perf_counter()
+    ref_gpu.build()
+    out = {"build_s": round(time.perf_counter() - t0, 1), "graphs": []}
+    for name in graphs:
+        desc, wl_name = REFGPU_GRAPHS[name]
+        g = make_graph(pg, WORKLOADS[wl_name], device)
+        rp, col = g.csr()
+        g.free()
+        n = rp.size - 1
+        used = np.flatnonzero(np.diff(rp) > 0)
+        n_file = int(used[-1]) + 1 if used.size else 0
+        entry = {"graph": desc, "n": n_file, "m_undirected": int(rp[-1]) // 2, "drivers": []}
+        with tempfile.TemporaryDirectory() as td:
+            path = os.path.join(td, name + ".mtx")
+            src = np.repeat(np.arange(n, dtype=np.int64), np.diff(rp))
+            up = src < col
+            e = np.stack([src[up] + 1, col[up].astype(np.int64) + 1], axis=1)
+            with open(path, "w") as f:
+                f.write("%%%%MatrixMarket matrix coordinate pattern symmetric\n%d %d %d\n" % (n, n, e.shape[0]))
+                np.savetxt(f, e, fmt="%d")
+            del src, up, e
+            drivers = list(ref_gpu.INDEX2CORE + ref_gpu.PEEL_VG)
+            if n_file < 1000000:
+                drivers += list(ref_gpu.DYN)
+            engines = {}
+            for d in drivers:
+                mode = "csr" if d in ref_gpu.DYN else "coo"
+                t1 = time.perf_counter()
+                r = ref_gpu.run(d, path, n_file, timeout=1800)
+                wall = time.perf_counter() - t1
+                if mode not in engines:
+                    engines[mode] = pg.Graph.from_mtx(path, mode, device=device)
+                h = engines[mode]
+                got, _ = h.decompose(d)
+                ms = []
+                for _ in range(5):
+                    h.decompose_device(d)
+                    ms.append(h.last_timing()[0])
+                e_ms = statistics.median(ms)
+                entry["drivers"].append({
+                    "driver": d, "reference_ms": r.ms, "engine_ms": round(e_ms, 4),
+                    "speedup": round(r.ms / e_ms, 1) if r.ms else None, "identical": bool(np.array_equal(got, r.core)),
+                    "reference_iterations": r.iterations, "reference_process_s": round(wall, 1)})
+            for h in engines.values():
+                h.free()
+        out["graphs"].append(entry)
+    return out
 
 
 def graph_section(pg, device, sptr, name, method, steps):
@@ -772,6 +847,9 @@ def main():
     ap.add_argument("--no-serve", action="store_true", help="skip the serving section")
     ap.add_argument("--no-inputs", action="store_true", help="skip the input/output path section")
     ap.add_argument("--no-c2", action="store_true", help="skip the R-MAT scale 22 section")
+    ap.add_argument("--no-refgpu", action="store_true", help="skip the reference GPU driver section")
+    ap.add_argument("--refgpu-graphs", default="er65536,rmat22",
+                    help="graphs of the reference GPU driver section (er65536, rmat22)")
     ap.add_argument("--batch-graphs", type=int, default=4096, help="graphs in the batched section")
     ap.add_argument("--no-autotune", action="store_true", help="batched section: keep the default configuration")
     ap.add_argument("--serve-requests", type=int, default=40)

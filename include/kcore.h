@@ -56,7 +56,7 @@ enum {
     KC_GPP = 4,         /* peel/gppeel.cu            bucket peel (+ deg0 -> 1) */
     KC_PEELONE_DYN = 5, /* peel/src/peelone-dyn.cc   bucket peel              */
     KC_PEEL_DYN = 6,    /* peel/src/peel-dyn.cc      bucket peel              */
-    KC_AUTO = 7         /* engine's choice (autotuned)                        */
+    KC_AUTO = 7         /* engine's choice: see kc_graph_autotune             */
 };
 
 /* MatrixMarket loader semantics. */
@@ -79,7 +79,12 @@ typedef struct kc_graph kc_graph;
 
 typedef struct kc_stats {
     uint32_t method;      /* method actually run */
-    uint32_t iterations;  /* peel: levels processed; h-index: sweeps */
+    /* peel: level indices processed; h-index: Gauss-Seidel sweeps.  The CLI
+     * drivers print this as "Number of iterations"; the reference prints its
+     * own synchronous schedule's count there (HistoCore.cu:346, CntCore.cu:421,
+     * NbrCore.cu:302, peelone.cu:191, gppeel.cu:231), which the engine's
+     * schedule does not follow, so the two numbers differ. */
+    uint32_t iterations;
     uint32_t levels;      /* peel: distinct non-empty levels (= distinct core values) */
     uint32_t kmax;        /* largest core number ("Max K") */
     uint32_t kmin;        /* reference's "Min K": min(10, smallest core) (util.cpp:6-22) */
@@ -185,6 +190,16 @@ int kc_graph_virtual_layout(kc_graph *g, uint32_t part_size, uint32_t *node_poin
  * (see kc_graph_device_core).  stats may be NULL. */
 int kc_decompose(kc_graph *g, int method, uint32_t *core_out, int out_on_device, kc_stats *stats,
                  void *stream);
+/* Chooses what KC_AUTO runs on this graph by timing it: the bucket peel
+ * with its default tunables, the peel with the other row-chunk size (1024 /
+ * 2048 entries), the peel keeping more cascade items per CTA ("peel.spill"
+ * 2 x + 16), and the h-index iteration, each warmed up once and timed twice;
+ * the fastest (method and peel tunables) is kept in the graph.  *method receives the chosen KC_*
+ * method, *best_ms its time (either may be NULL).  The first
+ * kc_decompose(KC_AUTO) of a graph calls this itself, so that call takes
+ * about eight decompositions longer; later KC_AUTO calls reuse the choice.
+ * No counterpart in the reference, which runs one fixed method per binary. */
+int kc_graph_autotune(kc_graph *g, int *method, double *best_ms);
 /* CUDA-event timings of the last decomposition on this graph: *total_ms
  * covers every kernel of the call (initialisation included), *kernel_ms the
  * main decomposition kernel alone.  Either pointer may be NULL. */

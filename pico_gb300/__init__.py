@@ -176,6 +176,7 @@ def lib():
     _sig(L, "kc_server_get_stats", i, [_P, ctypes.POINTER(kc_server_stats)])
     _sig(L, "kc_server_free", i, [_P])
     _sig(L, "kc_decompose_noalloc", i, [_P, _P, u32, _P, _P])
+    _sig(L, "kc_graph_autotune", i, [_P, ctypes.POINTER(i), ctypes.POINTER(ctypes.c_double)])
     _lib = L
     return L
 
@@ -397,6 +398,14 @@ class Graph:
         check(lib().kc_decompose(self._h, method_id(method), None, 0, ctypes.byref(st) if stats else None,
                                  ctypes.c_void_p(stream)))
         return _stats(st) if stats else None
+
+    def autotune(self):
+        """Times the peel variants and the h-index iteration on this graph
+        and keeps the fastest for method "auto"; returns (method name, ms)."""
+        m = ctypes.c_int()
+        ms = ctypes.c_double()
+        check(lib().kc_graph_autotune(self._h, ctypes.byref(m), ctypes.byref(ms)))
+        return method_name(m.value), ms.value
 
     def last_timing(self):
         """(total_ms, kernel_ms) of the last decomposition (CUDA events)."""

@@ -510,6 +510,68 @@ int kc_graph_virtual_layout(kc_graph *g, uint32_t part_size, uint32_t *node_poin
     return virtual_layout(g, part_size, node_pointer, edge_list, parts, num_parts);
 }
 
+namespace kc {
+
+// One decomposition by `method` (no stats, result stays on the device).
+static int run_method(Graph *g, int method, cudaStream_t s) {
+    if (g->n == 0) return KC_OK;
+    if (method == KC_HISTO || method == KC_CNT || method == KC_NBR) return hindex_run(g, s, nullptr);
+    return peel_run(g, s, method == KC_GPP, nullptr);
+}
+
+// The autotuner behind KC_AUTO: times the candidates on this graph -- the
+// bucket peel with its default tunables, the peel with the other row-chunk
+// size, the peel keeping more cascade items per CTA before it publishes them
+// to the shared queues, and the h-index iteration -- each
+// once to warm up and then twice, keeps the fastest (its method and peel
+// tunables) in the graph and restores nothing else.
+static int autotune_graph(Graph *g, cudaStream_t s) {
+    struct Cand {
+        int method;
+        int chunk;
+        int spill;
+    };
+    const Tuning base = g->tune;
+    const int other_chunk = (g->nnz >= (1ull << 29)) ? 1024 : 2048;
+    const Cand cands[] = {{KC_PEELONE_DYN, base.peel_chunk, base.peel_spill},
+                          {KC_PEELONE_DYN, other_chunk, base.peel_spill},
+                          {KC_PEELONE_DYN, base.peel_chunk, 2 * base.peel_spill + 16},
+                          {KC_NBR, base.peel_chunk, base.peel_spill}};
+    double best = 1e300;
+    Cand pick = cands[0];
+    for (const Cand &c : cands) {
+        g->tune.peel_chunk = c.chunk;
+        g->tune.peel_spill = c.spill;
+        double t = 1e300;
+        for (int rep = 0; rep < 3; rep++) {
+            KC_TRY(run_method(g, c.method, s));
+            if (rep > 0) t = std::min(t, g->last_ms);
+        }
+        if (t < best) {
+            best = t;
+            pick = c;
+        }
+    }
+    g->tune.peel_chunk = pick.chunk;
+    g->tune.peel_spill = pick.spill;
+    g->auto_method = pick.method;
+    g->auto_ms = best;
+    return KC_OK;
+}
+
+}  // namespace kc
+
+int kc_graph_autotune(kc_graph *g, int *method, double *best_ms) {
+    clear_error();
+    NvtxRange nvtx_("kc_graph_autotune");
+    if (!g) return fail(KC_ERR_INVALID, "null graph");
+    KC_CUDA(cudaSetDevice(g->device));
+    KC_TRY(autotune_graph(g, g->stream));
+    if (method) *method = g->auto_method;
+    if (best_ms) *best_ms = g->auto_ms;
+    return KC_OK;
+}
+
 int kc_decompose(kc_graph *g, int method, uint32_t *core_out, int out_on_device, kc_stats *stats, void *stream) {
     clear_error();
     NvtxRange nvtx_("kc_decompose");
@@ -519,7 +581,8 @@ int kc_decompose(kc_graph *g, int method, uint32_t *core_out, int out_on_device,
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : g->stream;
     kc_stats st;
     memset(&st, 0, sizeof(st));
-    int run = method == KC_AUTO ? KC_PEELONE_DYN : method;
+    if (method == KC_AUTO && g->auto_method < 0 && g->n) KC_TRY(autotune_graph(g, s));
+    int run = method == KC_AUTO ? (g->auto_method < 0 ? KC_PEELONE_DYN : g->auto_method) : method;
     st.method = (uint32_t)run;
     st.n = g->n;
     st.nnz = g->nnz;

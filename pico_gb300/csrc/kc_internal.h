@@ -170,6 +170,8 @@ struct Graph {
     unsigned long long *mcount = nullptr;
     bool simple_checked = false;
     std::vector<uint32_t> color_count;
+    int auto_method = -1;             // method KC_AUTO runs (set by the autotuner; -1: not tuned yet)
+    double auto_ms = 0.0;             // its time when it was tuned
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, evk0 = nullptr, evk1 = nullptr;
     double last_ms = 0.0, last_kernel_ms = 0.0;
 

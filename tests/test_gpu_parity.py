@@ -272,3 +272,21 @@ def test_hub_row_above_2_pow_24():
         assert np.array_equal(got, core), method
         assert st.kmax == kmax, method
     g.free()
+
+
+def test_auto_method_is_tuned_per_graph_and_exact():
+    """KC_AUTO: the first call times the peel variants and the h-index
+    iteration on the graph and keeps the fastest; every call, first and
+    later, gives the Batagelj-Zaversnik core numbers, and later calls run
+    the method the tuner chose."""
+    graphs = [pg.rmat_graph(16, 16, seed=3), pg.er_graph(20000, 200000, seed=4)]
+    for g in graphs:
+        rp, col = g.csr()
+        want, _ = oracle.bz(rp, col)
+        got, st = g.decompose("auto")
+        assert np.array_equal(got, want)
+        name, ms = g.autotune()
+        assert name in pg.METHODS and name != "auto" and ms > 0
+        got, st = g.decompose("auto")
+        assert np.array_equal(got, want) and st.method == name
+        g.free()

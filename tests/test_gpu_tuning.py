@@ -1,6 +1,7 @@
 """The peel's work-accounting protocol under extreme tunables: everything
 spilled to the shared queues, one item per steal, 1..64 queues, tiny and large
-row chunks, one CTA per SM, both CTA sizes and both unroll depths.  Every setting must give the exact core numbers."""
+row chunks, one CTA per SM, both CTA sizes and both unroll depths.  Every
+setting must give the exact core numbers."""
 import numpy as np
 import pytest
 
