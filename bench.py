@@ -59,6 +59,11 @@ WORKLOADS = {
     "rmat25planted": dict(kind="rmat_planted", scale=25, ef=16, k=4000, p=0.6, seed=3,
                           desc="R-MAT scale 25, edge factor 16 plus a planted 4000-vertex subgraph at p=0.6, "
                                "seed 3, de-duplicated, symmetrised; one graph per step"),
+    # the same construction at a quarter of the size: the case profiled with
+    # many-pass counter sets (a few GB on the device)
+    "rmat23planted": dict(kind="rmat_planted", scale=23, ef=16, k=4000, p=0.6, seed=3,
+                          desc="R-MAT scale 23, edge factor 16 plus a planted 4000-vertex subgraph at p=0.6, "
+                               "seed 3, de-duplicated, symmetrised; one graph per step"),
 }
 
 

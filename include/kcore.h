@@ -215,7 +215,9 @@ int kc_graph_last_timing(const kc_graph *g, double *total_ms, double *kernel_ms)
  * "peel.threads" (threads per CTA, 512 or 256), "peel.balanced" (1 = each
  * processing round spreads at most "peel.round_entries" row entries evenly
  * over the CTA's threads), "peel.scan_unroll" (alive-list entries per
- * thread per scan tile, 4 or 8), "hindex.warp_rows" (h-index: after the
+ * thread per scan tile, 4 or 8), "peel.aggregate" (1 = lanes of a warp that
+ * decrement the same vertex issue one atomicSub of their count; exact either
+ * way, off by default because it measured slower), "hindex.warp_rows" (h-index: after the
  * first sweep, rows up to this many entries are re-examined by one warp,
  * longer ones by a whole CTA; default 8192),
  * "trace" (1 = record a per-level trace of the next decompositions),

@@ -654,6 +654,8 @@ int kc_graph_set_param(kc_graph *g, const char *name, int64_t value) {
     } else if (k == "peel.round_entries") {
         if (value < 256 || value > (1 << 24)) return fail(KC_ERR_INVALID, "peel.round_entries: [256, 2^24]");
         t.peel_round_entries = (int)value;
+    } else if (k == "peel.aggregate") {
+        t.peel_aggregate = value ? 1 : 0;
     } else if (k == "peel.scan_unroll") {
         if (value != 4 && value != 8) return fail(KC_ERR_INVALID, "peel.scan_unroll: 4 or 8");
         t.peel_scan_unroll = (int)value;

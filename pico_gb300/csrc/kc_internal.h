@@ -107,6 +107,7 @@ struct Tuning {
     int peel_balanced = 1;   // 1: rounds spread a bounded number of row entries over the whole CTA
     int peel_round_entries = 16384;
     int peel_scan_unroll = 4;  // alive-list entries per thread per scan tile: 4 or 8
+    int peel_aggregate = 0;    // 1: warp-aggregated decrements (measured 5-9% slower: repeats within a warp are rare)
     int trace = 0;
     int64_t hindex_warp_rows = 8192;  // h-index: rows up to this length re-examined by one warp
     int64_t update_incremental_max = 512;  // larger update batches: full recompute (measured crossover ~1000 edges)

@@ -78,6 +78,7 @@ struct PeelArgs {
     unsigned nq;                 // shared queues in use
     unsigned round_e;            // balanced rounds: row entries a CTA takes per round
     unsigned withhold;           // CTA 0 keeps one credit of level index 1 (failure-detection hook)
+    unsigned aggregate;          // lanes of a warp decrementing the same vertex issue one atomicSub
 };
 
 // Initialisation and level 0 in one streaming pass: residual degrees from the
@@ -675,12 +676,29 @@ __global__ void __launch_bounds__(NT, 1024 / NT) peel_kernel(PeelArgs A) {
                             live[k] = !(w & (1u << (u[k] & 31)));
                         }
                     }
+                    // Warp-aggregated decrements: lanes holding the same
+                    // vertex (hubs shared by many short rows) form a group
+                    // whose lowest lane subtracts the group's size once.
+                    unsigned cnt[PEEL_U];
 #pragma unroll
-                    for (int k = 0; k < PEEL_U; k++) a[k] = live[k] ? atomicSub(&A.deg[u[k]], 1u) : 0u;
-                    // the decrement that moved u from L+1 to L claims it; the
-                    // claim atomics of all PEEL_U entries are in flight together
-                    // (with the row offsets of each candidate, so that its row
-                    // can be queued as a range item)
+                    for (int k = 0; k < PEEL_U; k++) {
+                        cnt[k] = 1u;
+                        if (A.aggregate) {
+                            const unsigned peers = __match_any_sync(KC_FULL_MASK, live[k] ? u[k] : 0xffffffffu);
+                            cnt[k] = __popc(peers);
+                            if ((int)lane != __ffs(peers) - 1) live[k] = false;
+                        }
+                    }
+#pragma unroll
+                    for (int k = 0; k < PEEL_U; k++) a[k] = live[k] ? atomicSub(&A.deg[u[k]], cnt[k]) : 0u;
+                    // The decrement (or group) that moved u from above L to L
+                    // or below claims it and lifts it back to exactly L; a
+                    // decrement that found u at or below L is undone (the
+                    // reference's clamp).  A residual degree never falls below
+                    // zero: it has lost at most one decrement per entry of its
+                    // row.  The claim atomics of all PEEL_U entries are in
+                    // flight together (with the row offsets of each candidate,
+                    // so that its row can be queued as a range item).
                     unsigned oldc[PEEL_U];
                     int64_t cr0[PEEL_U], cr1[PEEL_U];
 #pragma unroll
@@ -688,14 +706,16 @@ __global__ void __launch_bounds__(NT, 1024 / NT) peel_kernel(PeelArgs A) {
                         oldc[k] = ~0u;
                         cr0[k] = cr1[k] = 0;
                         if (live[k]) {
-                            if (a[k] == L + 1) {
+                            const unsigned nv = a[k] - cnt[k];
+                            if ((int)a[k] <= (int)L) {
+                                atomicAdd(&A.deg[u[k]], cnt[k]);
+                            } else if (nv <= L) {
                                 oldc[k] = atomicOr(&A.claimed[u[k] >> 5], 1u << (u[k] & 31));
                                 cr0[k] = A.rowptr[u[k]];
                                 cr1[k] = A.rowptr[u[k] + 1];
-                            } else if ((int)a[k] <= (int)L) {
-                                atomicAdd(&A.deg[u[k]], 1u);
+                                if (nv < L) atomicAdd(&A.deg[u[k]], L - nv);
                             } else {
-                                local_min = min(local_min, a[k] - 1);
+                                local_min = min(local_min, nv);
                             }
                         }
                     }
@@ -898,6 +918,7 @@ int peel_run(Graph *g, cudaStream_t s, bool gpp_zero_to_one_flag, kc_stats *st) 
     A.steal_max = (unsigned)g->tune.peel_steal;
     A.nq = nq_of(g);
     A.round_e = (unsigned)g->tune.peel_round_entries;
+    A.aggregate = (unsigned)g->tune.peel_aggregate;
     KC_CUDA(cudaEventRecord(g->ev0, s));
     if (A.trace) KC_CUDA(cudaMemsetAsync(g->trace, 0, sizeof(PeelTrace) * g->trace_cap, s));
     const int ig = std::max(1, std::min<int>(g->sm_count * 8, (int)((g->n + 255) / 256)));

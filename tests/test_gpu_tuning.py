@@ -1,7 +1,8 @@
 """The peel's work-accounting protocol under extreme tunables: everything
 spilled to the shared queues, one item per steal, 1..64 queues, tiny and large
-row chunks, one CTA per SM, both CTA sizes and both unroll depths.  Every
-setting must give the exact core numbers."""
+row chunks, one CTA per SM, both CTA sizes and both unroll depths, with and
+without warp-aggregated decrements.  Every setting must give the exact core
+numbers."""
 import numpy as np
 import pytest
 
@@ -32,6 +33,10 @@ SETTINGS = [
     {"peel.scan_unroll": 8},
     {"peel.scan_unroll": 8, "peel.balanced": 1, "peel.chunk": 512, "peel.round_entries": 16384},
     {"peel.scan_unroll": 8, "peel.threads": 256, "peel.unroll": 8, "peel.spill": 0},
+    {"peel.aggregate": 1},
+    {"peel.aggregate": 1, "peel.balanced": 0, "peel.unroll": 8, "peel.spill": 0, "peel.steal": 2},
+    {"peel.aggregate": 1, "peel.threads": 256, "peel.chunk": 256, "peel.round_entries": 256},
+    {"peel.aggregate": 0},
 ]
 
 
