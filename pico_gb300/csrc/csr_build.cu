@@ -186,30 +186,40 @@ __global__ void scatter_edges(const uint32_t *__restrict__ src, const uint32_t *
 }
 
 // ------------------------------------------------------ segmented sort ----
+// Rows are sorted by size class: up to 32 entries one warp per row (shuffle
+// bitonic network); 33..4096 entries padded to P = 2^k (k = 6..12) and sorted
+// SORT_PACK / P rows at a time per CTA in shared memory (one bitonic network,
+// so short rows share the barriers instead of occupying a CTA each); longer
+// rows one CTA per row with an LSD radix sort.
 constexpr uint32_t CLASS_A_MAX = 32;
 constexpr uint32_t CLASS_B_MAX = 4096;
+constexpr int SORT_BUCKETS = 9;  // 0: <= 32; 1..7: P = 64..4096; 8: > 4096
+constexpr uint32_t SORT_PACK = 1024;
 
-__global__ void classify_rows(const int64_t *__restrict__ rowptr, uint32_t n, uint32_t *la, uint32_t *lb,
-                              uint32_t *lc, unsigned long long *counts) {
+__device__ __forceinline__ int sort_bucket(int64_t len) {
+    if (len < 2) return -1;
+    if (len <= (int64_t)CLASS_A_MAX) return 0;
+    if (len > (int64_t)CLASS_B_MAX) return SORT_BUCKETS - 1;
+    int k = 6;
+    while (((int64_t)1 << k) < len) k++;
+    return k - 5;  // 64 -> 1, ..., 4096 -> 7
+}
+
+// Pass 1 (cursor == nullptr): rows per bucket into counts.  Pass 2: each row
+// id goes to list[cursor[bucket]++] (cursors start at the buckets' offsets).
+__global__ void classify_rows(const int64_t *__restrict__ rowptr, uint32_t n, unsigned long long *counts,
+                              unsigned long long *cursor, uint32_t *list) {
     const unsigned lane = threadIdx.x & 31;
     for (uint64_t base = blockIdx.x * (uint64_t)blockDim.x; base < n; base += (uint64_t)gridDim.x * blockDim.x) {
-        uint64_t v = base + threadIdx.x;
-        int cls = -1;
-        if (v < n) {
-            int64_t len = rowptr[v + 1] - rowptr[v];
-            if (len >= 2) cls = len <= CLASS_A_MAX ? 0 : (len <= CLASS_B_MAX ? 1 : 2);
-        }
-#pragma unroll
-        for (int c = 0; c < 3; c++) {
-            unsigned int b = __ballot_sync(KC_FULL_MASK, cls == c);
+        const uint64_t v = base + threadIdx.x;
+        const int cls = v < n ? sort_bucket(rowptr[v + 1] - rowptr[v]) : -1;
+        for (int c = 0; c < SORT_BUCKETS; c++) {
+            const unsigned b = __ballot_sync(KC_FULL_MASK, cls == c);
             if (!b) continue;
             unsigned long long pos = 0;
-            if (lane == 0) pos = atomicAdd(&counts[c], (unsigned long long)__popc(b));
+            if (lane == 0) pos = atomicAdd(cursor ? &cursor[c] : &counts[c], (unsigned long long)__popc(b));
             pos = __shfl_sync(KC_FULL_MASK, pos, 0);
-            if (cls == c) {
-                uint32_t *L = c == 0 ? la : (c == 1 ? lb : lc);
-                L[pos + __popc(b & ((1u << lane) - 1))] = (uint32_t)v;
-            }
+            if (cursor && cls == c) list[pos + __popc(b & ((1u << lane) - 1))] = (uint32_t)v;
         }
     }
 }
@@ -258,49 +268,66 @@ __global__ void sort_rows_warp(const int64_t *__restrict__ rowptr, const uint32_
     }
 }
 
-// Class B: one CTA per row of <= 4096 entries, shared-memory bitonic sort.
-template <bool HAS_VAL>
-__global__ void __launch_bounds__(512) sort_rows_block(const int64_t *__restrict__ rowptr,
-                                                       const uint32_t *__restrict__ rows, uint64_t nrows,
-                                                       uint32_t *key, uint32_t *val) {
-    __shared__ uint32_t sk[CLASS_B_MAX];
-    __shared__ uint32_t sv[HAS_VAL ? CLASS_B_MAX : 1];
-    for (uint64_t r = blockIdx.x; r < nrows; r += gridDim.x) {
-        uint32_t v = rows[r];
-        int64_t start = rowptr[v];
-        uint32_t len = (uint32_t)(rowptr[v + 1] - start);
-        uint32_t P = 64;
-        while (P < len) P <<= 1;
-        for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) {
-            sk[i] = i < len ? key[start + i] : 0xffffffffu;
-            if (HAS_VAL) sv[i] = i < len ? val[start + i] : 0xffffffffu;
+// Class B: rows of P/2 < len <= P entries (P = 2^LOGP, 64..4096), padded to
+// P with the largest key, SORT_PACK / P rows per CTA (one row for P > 1024).
+template <bool HAS_VAL, int LOGP>
+__global__ void __launch_bounds__(256) sort_rows_pack(const int64_t *__restrict__ rowptr,
+                                                      const uint32_t *__restrict__ rows, uint64_t nrows,
+                                                      uint32_t *key, uint32_t *val) {
+    constexpr uint32_t P = 1u << LOGP;
+    constexpr uint32_t E = P > SORT_PACK ? P : SORT_PACK;  // elements per CTA
+    constexpr uint32_t RPC = E / P;                          // rows per CTA
+    __shared__ uint32_t sk[E];
+    __shared__ uint32_t sv[HAS_VAL ? E : 1];
+    __shared__ int64_t rstart[RPC];
+    __shared__ uint32_t rlen[RPC];
+    for (uint64_t grp = blockIdx.x; grp * RPC < nrows; grp += gridDim.x) {
+        if (threadIdx.x < RPC) {
+            const uint64_t r = grp * RPC + threadIdx.x;
+            if (r < nrows) {
+                const uint32_t v = rows[r];
+                rstart[threadIdx.x] = rowptr[v];
+                rlen[threadIdx.x] = (uint32_t)(rowptr[v + 1] - rowptr[v]);
+            } else {
+                rstart[threadIdx.x] = 0;
+                rlen[threadIdx.x] = 0;
+            }
+        }
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < E; i += blockDim.x) {
+            const uint32_t j = i / P, o = i % P;
+            const bool in = o < rlen[j];
+            sk[i] = in ? key[rstart[j] + o] : 0xffffffffu;
+            if (HAS_VAL) sv[i] = in ? val[rstart[j] + o] : 0xffffffffu;
         }
         __syncthreads();
         for (uint32_t size = 2; size <= P; size <<= 1) {
             for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
-                for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) {
-                    uint32_t j = i ^ stride;
-                    if (j > i) {
-                        bool asc = (i & size) == 0;
-                        uint32_t ki = sk[i], kj = sk[j];
-                        uint32_t vi = HAS_VAL ? sv[i] : 0u, vj = HAS_VAL ? sv[j] : 0u;
-                        bool sw = asc ? kv_less<HAS_VAL>(kj, vj, ki, vi) : kv_less<HAS_VAL>(ki, vi, kj, vj);
-                        if (sw) {
-                            sk[i] = kj;
-                            sk[j] = ki;
-                            if (HAS_VAL) {
-                                sv[i] = vj;
-                                sv[j] = vi;
-                            }
+                for (uint32_t q = threadIdx.x; q < E / 2; q += blockDim.x) {
+                    const uint32_t i = 2 * stride * (q / stride) + (q % stride);
+                    const uint32_t j = i + stride;
+                    const bool asc = ((i & (P - 1)) & size) == 0;
+                    const uint32_t ki = sk[i], kj = sk[j];
+                    const uint32_t vi = HAS_VAL ? sv[i] : 0u, vj = HAS_VAL ? sv[j] : 0u;
+                    const bool sw = asc ? kv_less<HAS_VAL>(kj, vj, ki, vi) : kv_less<HAS_VAL>(ki, vi, kj, vj);
+                    if (sw) {
+                        sk[i] = kj;
+                        sk[j] = ki;
+                        if (HAS_VAL) {
+                            sv[i] = vj;
+                            sv[j] = vi;
                         }
                     }
                 }
                 __syncthreads();
             }
         }
-        for (uint32_t i = threadIdx.x; i < len; i += blockDim.x) {
-            key[start + i] = sk[i];
-            if (HAS_VAL) val[start + i] = sv[i];
+        for (uint32_t i = threadIdx.x; i < E; i += blockDim.x) {
+            const uint32_t j = i / P, o = i % P;
+            if (o < rlen[j]) {
+                key[rstart[j] + o] = sk[i];
+                if (HAS_VAL) val[rstart[j] + o] = sv[i];
+            }
         }
         __syncthreads();
     }
@@ -389,51 +416,73 @@ __global__ void __launch_bounds__(RADIX_THREADS) sort_rows_radix(const int64_t *
     }
 }
 
+template <bool HAS_VAL>
+static void launch_pack(int logp, const int64_t *rowptr, const uint32_t *rows, uint64_t nrows, uint32_t *key,
+                        uint32_t *val, int sms, cudaStream_t s) {
+    const uint64_t rpc = logp >= 10 ? 1 : (SORT_PACK >> logp);
+    const int gr = (int)std::max<uint64_t>(1, std::min<uint64_t>((nrows + rpc - 1) / rpc, (uint64_t)sms * 8));
+    switch (logp) {
+    case 6: sort_rows_pack<HAS_VAL, 6><<<gr, 256, 0, s>>>(rowptr, rows, nrows, key, val); break;
+    case 7: sort_rows_pack<HAS_VAL, 7><<<gr, 256, 0, s>>>(rowptr, rows, nrows, key, val); break;
+    case 8: sort_rows_pack<HAS_VAL, 8><<<gr, 256, 0, s>>>(rowptr, rows, nrows, key, val); break;
+    case 9: sort_rows_pack<HAS_VAL, 9><<<gr, 256, 0, s>>>(rowptr, rows, nrows, key, val); break;
+    case 10: sort_rows_pack<HAS_VAL, 10><<<gr, 256, 0, s>>>(rowptr, rows, nrows, key, val); break;
+    case 11: sort_rows_pack<HAS_VAL, 11><<<gr, 256, 0, s>>>(rowptr, rows, nrows, key, val); break;
+    default: sort_rows_pack<HAS_VAL, 12><<<gr, 256, 0, s>>>(rowptr, rows, nrows, key, val); break;
+    }
+}
+
 static int sort_rows(Graph *g, uint32_t *key, uint32_t *val, uint32_t max_key, cudaStream_t s) {
     const uint32_t n = g->n;
     if (n == 0 || g->nnz == 0) return KC_OK;
     const int sms = current_sms();
-    uint32_t *lists = nullptr;
+    uint32_t *list = nullptr;
     unsigned long long *counts = nullptr;
-    KC_TRY(dalloc(&lists, 3ull * n, "row class lists"));
-    if (dalloc(&counts, 3, "row class counts") != KC_OK) { dfree(lists); return KC_ERR_NOMEM; }
-    cudaMemsetAsync(counts, 0, 3 * sizeof(unsigned long long), s);
-    uint32_t *la = lists, *lb = lists + n, *lc = lists + 2ull * n;
-    classify_rows<<<grid_for(n, 256, sms), 256, 0, s>>>(g->rowptr, n, la, lb, lc, counts);
-    unsigned long long h[3];
+    KC_TRY(dalloc(&list, (uint64_t)n, "row class list"));
+    if (dalloc(&counts, 2 * SORT_BUCKETS, "row class counts") != KC_OK) { dfree(list); return KC_ERR_NOMEM; }
+    unsigned long long *cursor = counts + SORT_BUCKETS;
+    cudaMemsetAsync(counts, 0, SORT_BUCKETS * sizeof(unsigned long long), s);
+    classify_rows<<<grid_for(n, 256, sms), 256, 0, s>>>(g->rowptr, n, counts, nullptr, nullptr);
+    unsigned long long h[SORT_BUCKETS], off[SORT_BUCKETS + 1];
     cudaMemcpyAsync(h, counts, sizeof(h), cudaMemcpyDeviceToHost, s);
     cudaError_t e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) { dfree(lists); dfree(counts); return fail(KC_ERR_CUDA, "classify: %s", cudaGetErrorString(e)); }
+    if (e != cudaSuccess) { dfree(list); dfree(counts); return fail(KC_ERR_CUDA, "classify: %s", cudaGetErrorString(e)); }
+    off[0] = 0;
+    for (int c = 0; c < SORT_BUCKETS; c++) off[c + 1] = off[c] + h[c];
+    cudaMemcpyAsync(cursor, off, SORT_BUCKETS * sizeof(unsigned long long), cudaMemcpyHostToDevice, s);
+    classify_rows<<<grid_for(n, 256, sms), 256, 0, s>>>(g->rowptr, n, nullptr, cursor, list);
     const bool hv = val != nullptr;
     if (h[0]) {
         int gr = grid_for(h[0] * 32, 256, sms);
-        if (hv) sort_rows_warp<true><<<gr, 256, 0, s>>>(g->rowptr, la, h[0], key, val);
-        else sort_rows_warp<false><<<gr, 256, 0, s>>>(g->rowptr, la, h[0], key, val);
+        if (hv) sort_rows_warp<true><<<gr, 256, 0, s>>>(g->rowptr, list, h[0], key, val);
+        else sort_rows_warp<false><<<gr, 256, 0, s>>>(g->rowptr, list, h[0], key, val);
     }
-    if (h[1]) {
-        int gr = (int)std::min<unsigned long long>(h[1], (unsigned long long)sms * 8);
-        if (hv) sort_rows_block<true><<<gr, 512, 0, s>>>(g->rowptr, lb, h[1], key, val);
-        else sort_rows_block<false><<<gr, 512, 0, s>>>(g->rowptr, lb, h[1], key, val);
+    for (int c = 1; c < SORT_BUCKETS - 1; c++) {
+        if (!h[c]) continue;
+        if (hv) launch_pack<true>(c + 5, g->rowptr, list + off[c], h[c], key, val, sms, s);
+        else launch_pack<false>(c + 5, g->rowptr, list + off[c], h[c], key, val, sms, s);
     }
     uint32_t *tk = nullptr, *tv = nullptr;
     int rc = KC_OK;
-    if (h[2]) {
+    const unsigned long long hc = h[SORT_BUCKETS - 1];
+    if (hc) {
         int bits = 1;
         while (bits < 32 && (max_key >> bits) != 0) bits++;
         int passes = (bits + 7) / 8;
         rc = dalloc(&tk, g->nnz, "radix staging keys");
         if (rc == KC_OK && hv) rc = dalloc(&tv, g->nnz, "radix staging values");
         if (rc == KC_OK) {
-            int gr = (int)std::min<unsigned long long>(h[2], (unsigned long long)sms * 4);
-            if (hv) sort_rows_radix<true><<<gr, RADIX_THREADS, 0, s>>>(g->rowptr, lc, h[2], key, val, tk, tv, passes);
-            else sort_rows_radix<false><<<gr, RADIX_THREADS, 0, s>>>(g->rowptr, lc, h[2], key, val, tk, tv, passes);
+            const uint32_t *lc = list + off[SORT_BUCKETS - 1];
+            int gr = (int)std::min<unsigned long long>(hc, (unsigned long long)sms * 4);
+            if (hv) sort_rows_radix<true><<<gr, RADIX_THREADS, 0, s>>>(g->rowptr, lc, hc, key, val, tk, tv, passes);
+            else sort_rows_radix<false><<<gr, RADIX_THREADS, 0, s>>>(g->rowptr, lc, hc, key, val, tk, tv, passes);
         }
     }
     e = cudaGetLastError();
     cudaError_t e2 = cudaStreamSynchronize(s);
     dfree(tk);
     dfree(tv);
-    dfree(lists);
+    dfree(list);
     dfree(counts);
     if (rc != KC_OK) return rc;
     if (e != cudaSuccess || e2 != cudaSuccess)
@@ -442,35 +491,112 @@ static int sort_rows(Graph *g, uint32_t *key, uint32_t *val, uint32_t max_key, c
 }
 
 // ----------------------------------------------------------- unique -------
-__global__ void unique_count(const int64_t *__restrict__ rowptr, const uint32_t *__restrict__ col, uint32_t n,
-                             uint32_t *newdeg) {
-    const unsigned lane = threadIdx.x & 31;
-    uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
-    uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-    for (uint64_t v = warp; v < n; v += nwarps) {
-        int64_t s = rowptr[v], e = rowptr[v + 1];
-        uint32_t cnt = 0;
-        for (int64_t j = s + lane; j < e; j += 32) cnt += (j == s || col[j] != col[j - 1]) ? 1u : 0u;
-        cnt = __reduce_add_sync(KC_FULL_MASK, cnt);
-        if (lane == 0) newdeg[v] = cnt;
+// De-duplication of sorted rows, entry-parallel: an entry is kept when it
+// starts its row or differs from its predecessor.  Row starts are first set
+// in a bitmap over the entries (one thread per row), so a tile of UQ_TILE
+// entries (UQ_PER consecutive entries per thread) reads them with its entries
+// whatever the number of rows, empty ones included, that start in it.  Pass 1
+// counts the kept entries of each tile; a scan gives each tile its output
+// offset; pass 2 writes the kept entries and saves, per thread, its kept mask
+// and the kept count before it in the tile; a pass over the rows then gives
+// each row its new offset from those.
+constexpr unsigned UQ_THREADS = 256;
+constexpr unsigned UQ_PER = 16;
+constexpr unsigned UQ_TILE = UQ_THREADS * UQ_PER;
+
+__global__ void mark_row_starts(const int64_t *__restrict__ rowptr, uint32_t n, uint32_t *startbits) {
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n; v += (uint64_t)gridDim.x * blockDim.x) {
+        const int64_t r = rowptr[v];
+        if (rowptr[v + 1] > r) atomicOr(&startbits[r >> 5], 1u << (r & 31));
     }
 }
 
-__global__ void unique_compact(const int64_t *__restrict__ rowptr, const uint32_t *__restrict__ col, uint32_t n,
-                               const int64_t *__restrict__ nrowptr, uint32_t *ncol) {
-    const unsigned lane = threadIdx.x & 31;
-    uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
-    uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-    for (uint64_t v = warp; v < n; v += nwarps) {
-        int64_t s = rowptr[v], e = rowptr[v + 1];
-        int64_t w = nrowptr[v];
-        for (int64_t base = s; base < e; base += 32) {
-            int64_t j = base + lane;
-            bool keep = j < e && (j == s || col[j] != col[j - 1]);
-            unsigned int b = __ballot_sync(KC_FULL_MASK, keep);
-            if (keep) ncol[w + __popc(b & ((1u << lane) - 1u))] = col[j];
-            w += __popc(b);
+// Kept mask of this thread's UQ_PER entries of tile [t0, t0 + len) (bit i:
+// entry t0 + threadIdx.x * UQ_PER + i).
+__device__ __forceinline__ unsigned uq_mask(const uint32_t *__restrict__ col, const uint32_t *__restrict__ startbits,
+                                            uint64_t t0, unsigned len) {
+    unsigned mask = 0;
+    const unsigned o0 = threadIdx.x * UQ_PER;
+    if (o0 < len) {
+        const uint64_t e0 = t0 + o0;  // a multiple of UQ_PER: the bits lie in one word
+        const unsigned sb = (startbits[e0 >> 5] >> (e0 & 31)) & ((1u << UQ_PER) - 1u);
+        uint32_t prev = e0 > 0 ? col[e0 - 1] : 0u;
+#pragma unroll
+        for (unsigned i = 0; i < UQ_PER; i++) {
+            if (o0 + i < len) {
+                const uint32_t x = col[e0 + i];
+                if (((sb >> i) & 1u) || x != prev) mask |= 1u << i;
+                prev = x;
+            }
         }
+    }
+    return mask;
+}
+
+__global__ void __launch_bounds__(UQ_THREADS) unique_tiles_count(const uint32_t *__restrict__ col,
+                                                                  const uint32_t *__restrict__ startbits, uint64_t nnz,
+                                                                  uint32_t *tile_cnt) {
+    __shared__ uint32_t wsum[UQ_THREADS / 32];
+    const uint64_t tiles = (nnz + UQ_TILE - 1) / UQ_TILE;
+    for (uint64_t t = blockIdx.x; t < tiles; t += gridDim.x) {
+        const uint64_t t0 = t * UQ_TILE;
+        const unsigned len = (unsigned)(nnz - t0 < (uint64_t)UQ_TILE ? nnz - t0 : (uint64_t)UQ_TILE);
+        const unsigned c = __reduce_add_sync(KC_FULL_MASK, (unsigned)__popc(uq_mask(col, startbits, t0, len)));
+        if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = c;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned tot = 0;
+            for (unsigned w = 0; w < UQ_THREADS / 32; w++) tot += wsum[w];
+            tile_cnt[t] = tot;
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(UQ_THREADS) unique_tiles_write(const uint32_t *__restrict__ col,
+                                                                  const uint32_t *__restrict__ startbits, uint64_t nnz,
+                                                                  const int64_t *__restrict__ tile_off, uint32_t *ncol,
+                                                                  uint16_t *tmask, uint16_t *tpre) {
+    __shared__ uint32_t wsum[UQ_THREADS / 32];
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint64_t tiles = (nnz + UQ_TILE - 1) / UQ_TILE;
+    for (uint64_t t = blockIdx.x; t < tiles; t += gridDim.x) {
+        const uint64_t t0 = t * UQ_TILE;
+        const unsigned len = (unsigned)(nnz - t0 < (uint64_t)UQ_TILE ? nnz - t0 : (uint64_t)UQ_TILE);
+        const unsigned mask = uq_mask(col, startbits, t0, len);
+        unsigned wt;
+        const unsigned ex = warp_excl_scan((unsigned)__popc(mask), lane, wt);
+        if (lane == 0) wsum[warp] = wt;
+        __syncthreads();
+        unsigned before = 0;
+        for (unsigned w = 0; w < warp; w++) before += wsum[w];
+        const int64_t base = tile_off[t] + before + ex;
+        tmask[t * UQ_THREADS + threadIdx.x] = (uint16_t)mask;
+        tpre[t * UQ_THREADS + threadIdx.x] = (uint16_t)(before + ex);
+        const uint64_t e0 = t0 + threadIdx.x * UQ_PER;
+        unsigned k = 0;
+#pragma unroll
+        for (unsigned i = 0; i < UQ_PER; i++)
+            if ((mask >> i) & 1u) ncol[base + k++] = col[e0 + i];
+        __syncthreads();
+    }
+}
+
+// New offset of every row: the kept entries before its old start.
+__global__ void unique_rows(const int64_t *__restrict__ rowptr, uint32_t n, uint64_t nnz,
+                            const int64_t *__restrict__ tile_off, const uint16_t *__restrict__ tmask,
+                            const uint16_t *__restrict__ tpre, int64_t *nrow) {
+    const uint64_t tiles = (nnz + UQ_TILE - 1) / UQ_TILE;
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v <= n; v += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t r = (uint64_t)rowptr[v];
+        if (r >= nnz) {
+            nrow[v] = tile_off[tiles];
+            continue;
+        }
+        const uint64_t t = r / UQ_TILE;
+        const unsigned o = (unsigned)(r % UQ_TILE);
+        const uint64_t th = t * UQ_THREADS + o / UQ_PER;
+        nrow[v] = tile_off[t] + tpre[th] + __popc((unsigned)tmask[th] & ((1u << (o % UQ_PER)) - 1u));
     }
 }
 
@@ -556,21 +682,40 @@ int build_csr_from_edges(Graph *g, const uint32_t *d_src, const uint32_t *d_dst,
     }
     dfree(key);
     if (rc) { dfree(deg); dfree(err); return rc; }
-    if (flags & KC_EDGES_DEDUP) {
-        int64_t *nrow = nullptr;
-        uint32_t *ncol = nullptr;
+    if ((flags & KC_EDGES_DEDUP) && g->nnz) {
+        int64_t *nrow = nullptr, *toff = nullptr;
+        uint32_t *ncol = nullptr, *tcnt = nullptr, *sbits = nullptr;
+        uint16_t *tmask = nullptr, *tpre = nullptr;
+        const uint64_t tiles = (g->nnz + UQ_TILE - 1) / UQ_TILE;
+        auto release = [&]() {
+            dfree(tcnt);
+            dfree(toff);
+            dfree(sbits);
+            dfree(tmask);
+            dfree(tpre);
+        };
         rc = dalloc(&nrow, (uint64_t)n + 1, "dedup row offsets");
-        if (rc) { dfree(deg); dfree(err); return rc; }
-        if (n) unique_count<<<grid_for((uint64_t)n * 32, 256, sms), 256, 0, s>>>(g->rowptr, g->col, n, deg);
-        rc = exclusive_scan_u32_i64(deg, nrow, n, s);
+        if (rc == KC_OK) rc = dalloc(&tcnt, tiles, "dedup tile counts");
+        if (rc == KC_OK) rc = dalloc(&toff, tiles + 1, "dedup tile offsets");
+        if (rc == KC_OK) rc = dalloc(&sbits, tiles * (UQ_TILE / 32), "row-start bitmap");
+        if (rc == KC_OK) rc = dalloc(&tmask, tiles * UQ_THREADS, "dedup masks");
+        if (rc == KC_OK) rc = dalloc(&tpre, tiles * UQ_THREADS, "dedup prefixes");
+        if (rc) { release(); dfree(nrow); dfree(deg); dfree(err); return rc; }
+        cudaMemsetAsync(sbits, 0, tiles * (UQ_TILE / 32) * sizeof(uint32_t), s);
+        mark_row_starts<<<grid_for(n, 256, sms), 256, 0, s>>>(g->rowptr, n, sbits);
+        const int ug = (int)std::min<uint64_t>(tiles, (uint64_t)sms * 8);
+        unique_tiles_count<<<ug, UQ_THREADS, 0, s>>>(g->col, sbits, g->nnz, tcnt);
+        rc = exclusive_scan_u32_i64(tcnt, toff, tiles, s);
         int64_t nn = 0;
         if (rc == KC_OK) {
-            cudaMemcpy(&nn, nrow + n, 8, cudaMemcpyDeviceToHost);
+            cudaMemcpy(&nn, toff + tiles, 8, cudaMemcpyDeviceToHost);
             rc = dalloc(&ncol, (uint64_t)nn + 1, "dedup column ids");
         }
-        if (rc) { dfree(nrow); dfree(deg); dfree(err); return rc; }
-        if (n) unique_compact<<<grid_for((uint64_t)n * 32, 256, sms), 256, 0, s>>>(g->rowptr, g->col, n, nrow, ncol);
+        if (rc) { release(); dfree(nrow); dfree(deg); dfree(err); return rc; }
+        unique_tiles_write<<<ug, UQ_THREADS, 0, s>>>(g->col, sbits, g->nnz, toff, ncol, tmask, tpre);
+        unique_rows<<<grid_for((uint64_t)n + 1, 256, sms), 256, 0, s>>>(g->rowptr, n, g->nnz, toff, tmask, tpre, nrow);
         e = cudaStreamSynchronize(s);
+        release();
         dfree(g->rowptr);
         dfree(g->col);
         g->rowptr = nrow;

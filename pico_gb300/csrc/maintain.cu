@@ -179,18 +179,48 @@ __global__ void copy_runs(const uint32_t *__restrict__ col, uint64_t nnz_old, co
     }
 }
 
-// Writes the changed rows (one warp per listed row).
-__global__ void merge_write(const int64_t *__restrict__ rowptr, const uint32_t *__restrict__ col,
-                            const uint32_t *__restrict__ changed, uint32_t nchanged,
-                            const int64_t *__restrict__ drp, const uint32_t *__restrict__ dpos,
-                            const uint32_t *__restrict__ dcnt, const int64_t *__restrict__ irp,
-                            const uint32_t *__restrict__ ival, const uint32_t *__restrict__ icnt,
-                            const int64_t *__restrict__ nrow, uint32_t *ncol) {
+// The changed rows are written in chunks of MERGE_CHUNK old entries, one warp
+// per chunk, so a long row (deletions drawn from the edge set land on hub
+// rows of 10^5 entries) spreads over many warps instead of holding one warp
+// for the whole update.  nchunks[i] = chunks of changed row i (at least one,
+// so that a row that only gains entries still writes them).
+constexpr uint32_t MERGE_CHUNK = 1024;
+__global__ void merge_chunk_counts(const int64_t *__restrict__ rowptr, const uint32_t *__restrict__ changed,
+                                   uint32_t nchanged, uint32_t *nchunks) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nchanged;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t v = changed[i];
+        const uint64_t len = (uint64_t)(rowptr[v + 1] - rowptr[v]);
+        const uint64_t k = (len + MERGE_CHUNK - 1) / MERGE_CHUNK;
+        nchunks[i] = (uint32_t)(k > 0 ? k : 1);
+    }
+}
+
+// Chunk ci of the concatenated chunk lists (cstart: exclusive prefix of
+// nchunks, cstart[nchanged] = total): kept old entries p of its range move to
+// w0 + p - (deleted entries before p) + (inserted values below row[p]); the
+// row's inserted values are shared out over its chunks.
+__global__ void merge_write_chunks(const int64_t *__restrict__ rowptr, const uint32_t *__restrict__ col,
+                                   const uint32_t *__restrict__ changed, uint32_t nchanged,
+                                   const int64_t *__restrict__ cstart, uint64_t nch,
+                                   const int64_t *__restrict__ drp, const uint32_t *__restrict__ dpos,
+                                   const uint32_t *__restrict__ dcnt, const int64_t *__restrict__ irp,
+                                   const uint32_t *__restrict__ ival, const uint32_t *__restrict__ icnt,
+                                   const int64_t *__restrict__ nrow, uint32_t *ncol) {
     const unsigned lane = threadIdx.x & 31;
     const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
     const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-    for (uint64_t ci = warp; ci < nchanged; ci += nw) {
-        const uint32_t v = changed[ci];
+    for (uint64_t ci = warp; ci < nch; ci += nw) {
+        // changed row of this chunk: the last i with cstart[i] <= ci
+        uint32_t lo = 0, hi = nchanged;
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if ((uint64_t)cstart[mid] <= ci) lo = mid;
+            else hi = mid;
+        }
+        const uint32_t v = changed[lo];
+        const uint32_t c = (uint32_t)(ci - (uint64_t)cstart[lo]);
+        const uint32_t nc = (uint32_t)(cstart[lo + 1] - cstart[lo]);
         const int64_t r0 = rowptr[v];
         const uint32_t len = (uint32_t)(rowptr[v + 1] - r0);
         const int64_t w0 = nrow[v];
@@ -198,18 +228,15 @@ __global__ void merge_write(const int64_t *__restrict__ rowptr, const uint32_t *
         const uint32_t *dp = dc ? dpos + drp[v] : nullptr;
         const uint32_t *iv = ic ? ival + irp[v] : nullptr;
         const uint32_t *row = col + r0;
-        if (dc == 0 && ic == 0) {
-            for (uint32_t p = lane; p < len; p += 32) ncol[w0 + p] = row[p];
-            continue;
-        }
-        for (uint32_t p = lane; p < len; p += 32) {
+        const uint32_t p_end = min(len, (c + 1) * MERGE_CHUNK);
+        for (uint32_t p = c * MERGE_CHUNK + lane; p < p_end; p += 32) {
             const uint32_t x = row[p];
             const uint32_t before_d = dc ? lower_bound_u32(dp, dc, p) : 0u;
             if (before_d < dc && dp[before_d] == p) continue;  // deleted
             const uint32_t before_i = ic ? lower_bound_u32(iv, ic, x) : 0u;
             ncol[w0 + p - before_d + before_i] = x;
         }
-        for (uint32_t j = lane; j < ic; j += 32) {
+        for (uint32_t j = c * 32 + lane; j < ic; j += nc * 32) {
             const uint32_t y = iv[j];
             const uint32_t lb = lower_bound_u32(row, len, y);
             const uint32_t before_d = dc ? lower_bound_u32(dp, dc, lb) : 0u;
@@ -402,12 +429,22 @@ static int apply_changes(Graph *g, const uint32_t *d_isrc, const uint32_t *d_ids
     if (R)
         merge_plan<<<gw, 256, 0, s>>>(g->rowptr, g->col, changed, R, drp, md ? dg.col : nullptr, irp,
                                       mi ? ig.col : nullptr, dpos, dcnt, ival, icnt, newlen, applied);
+    // chunks of the changed rows for the merge
+    uint32_t *nchunks = nullptr;
+    int64_t *cstart = nullptr;
+    KC_TRY(sc.get(&nchunks, (uint64_t)R + 1, "merge chunk counts"));
+    KC_TRY(sc.get(&cstart, (uint64_t)R + 1, "merge chunk starts"));
+    if (R) {
+        merge_chunk_counts<<<grid_of(g, R), 256, 0, s>>>(g->rowptr, changed, R, nchunks);
+        KC_TRY(exclusive_scan_u32_i64(nchunks, cstart, R, s));
+    }
     int64_t *rp_new = nullptr;
     KC_TRY(dalloc(&rp_new, (uint64_t)n + 1, "row offsets"));
     int rc = exclusive_scan_u32_i64(newlen, rp_new, n, s);
-    int64_t nnz_new = 0;
+    int64_t nnz_new = 0, nch = 0;
     if (!rc) {
         cudaMemcpyAsync(&nnz_new, rp_new + n, 8, cudaMemcpyDeviceToHost, s);
+        if (R) cudaMemcpyAsync(&nch, cstart + R, 8, cudaMemcpyDeviceToHost, s);
         cudaError_t e0 = cudaStreamSynchronize(s);
         if (e0 != cudaSuccess) rc = fail(KC_ERR_CUDA, "CSR merge plan: %s", cudaGetErrorString(e0));
     }
@@ -421,9 +458,10 @@ static int apply_changes(Graph *g, const uint32_t *d_isrc, const uint32_t *d_ids
                 const int cb = (int)std::min<uint64_t>(tiles, (uint64_t)g->sm_count * 16);
                 copy_runs<<<cb, 256, 0, s>>>(g->col, g->nnz, ra, rb, rd, R, col_new);
             }
-            if (R)
-                merge_write<<<gw, 256, 0, s>>>(g->rowptr, g->col, changed, R, drp, dpos, dcnt, irp, ival, icnt, rp_new,
-                                               col_new);
+            if (R && nch > 0)
+                merge_write_chunks<<<grid_of(g, (uint64_t)nch * 32), 256, 0, s>>>(
+                    g->rowptr, g->col, changed, R, cstart, (uint64_t)nch, drp, dpos, dcnt, irp, ival, icnt, rp_new,
+                    col_new);
             unsigned long long h[2];
             cudaMemcpyAsync(h, applied, 16, cudaMemcpyDeviceToHost, s);
             cudaError_t e = cudaStreamSynchronize(s);
