@@ -195,7 +195,7 @@ def test_config1_er_65536_1m():
     g = pg.er_graph(65536, 1048576, seed=1)
     assert g.n == 65536 and g.nnz == 2 * 1048576
     rp, col = g.csr()
-    check_all_methods(g, rp, col, ["peelone_dyn", "NbrCore", "HistoCore", "gppeel"])
+    check_all_methods(g, rp, col, ALL + ["auto"])
     assert g.validate() == 0
 
 
@@ -204,9 +204,11 @@ def test_config2_rmat22_ef16():
     rp, col = g.csr()
     assert g.n == 1 << 22 and g.validate() == 0
     core, kmax = oracle.bz(rp, col)
-    for m in ("peelone_dyn", "NbrCore"):
+    # every method at full size (they share kernels, which is what this guards)
+    for m in ALL + ["auto"]:
         got, st = g.decompose(m)
-        assert np.array_equal(got, core), m
+        want = expected(m, core, rp)
+        assert np.array_equal(got, want), m
         assert st.kmax == kmax
     # the h-index sweeps race lowered estimates against pending-bit updates;
     # repeated runs vary the interleaving
@@ -225,6 +227,10 @@ def test_config3_rmat25_planted_core():
     core, kmax = oracle.bz(rp, col)
     assert np.array_equal(got, core)
     assert st.kmax == kmax and kmax >= 2000  # the planted core dominates
+    for m in ALL:
+        got, st = g.decompose(m)
+        assert np.array_equal(got, expected(m, core, rp)), m
+        assert st.kmax == kmax
     for _ in range(6):
         got_h, _ = g.decompose("NbrCore")
         assert np.array_equal(got_h, core)
