@@ -219,7 +219,13 @@ int kc_graph_last_timing(const kc_graph *g, double *total_ms, double *kernel_ms)
  * decrement the same vertex issue one atomicSub of their count; exact either
  * way, off by default because it measured slower), "hindex.warp_rows" (h-index: after the
  * first sweep, rows up to this many entries are re-examined by one warp,
- * longer ones by a whole CTA; default 8192),
+ * longer ones by a whole CTA; default 8192), "hindex.order" (1 = each
+ * h-index decomposition first copies the rows above "hindex.order_min"
+ * entries with the neighbours in descending buckets of floor(log2(degree)),
+ * so that its passes read only the prefix of a row that can hold the values
+ * they need; default 1; the copy takes 5 bytes per row entry and about 1 byte
+ * per entry more for the bucket table), "hindex.order_min" (default 128,
+ * at least 128),
  * "trace" (1 = record a per-level trace of the next decompositions),
  * "update.incremental_max" (largest update batch, in edges, maintained
  * incrementally by kc_graph_update), "wait.timeout_us" (limit of one

@@ -165,6 +165,11 @@ Graph::~Graph() {
     }
     dfree(hctl);
     dfree(hx_bitmap);
+    dfree(hx_ord);
+    dfree(hx_lid);
+    dfree(hx_pref);
+    dfree(hx_bk);
+    dfree(hx_vb);
     dfree(red);
     dfree(trace);
     dfree(mfront[0]);
@@ -662,6 +667,11 @@ int kc_graph_set_param(kc_graph *g, const char *name, int64_t value) {
     } else if (k == "hindex.warp_rows") {
         if (value < 512 || value > (int64_t)1 << 30) return fail(KC_ERR_INVALID, "hindex.warp_rows: [512, 2^30]");
         t.hindex_warp_rows = value;
+    } else if (k == "hindex.order") {
+        t.hindex_order = value ? 1 : 0;
+    } else if (k == "hindex.order_min") {
+        if (value < 128 || value > (int64_t)1 << 30) return fail(KC_ERR_INVALID, "hindex.order_min: [128, 2^30]");
+        t.hindex_order_min = value;
     } else if (k == "trace") {
         t.trace = value ? 1 : 0;
     } else if (k == "update.incremental_max") {

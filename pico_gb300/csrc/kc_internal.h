@@ -110,6 +110,8 @@ struct Tuning {
     int peel_aggregate = 0;    // 1: warp-aggregated decrements (measured 5-9% slower: repeats within a warp are rare)
     int trace = 0;
     int64_t hindex_warp_rows = 8192;  // h-index: rows up to this length re-examined by one warp
+    int hindex_order = 1;  // h-index: long rows read from a copy ordered by neighbour degree (prefix reads)
+    int64_t hindex_order_min = 128;  // h-index: rows above this length get the ordered copy
     int64_t update_incremental_max = 512;  // larger update batches: full recompute (measured crossover ~1000 edges)
     int64_t wait_timeout_us = 2000000;       // limit of one inter-CTA wait
     int withhold = 0;  // failure-detection hook: one CTA never signals, so the others' waits run out
@@ -130,6 +132,8 @@ struct HindexCtl {
     unsigned int changed;
     unsigned int err;
     unsigned int err_info;
+    unsigned long long ord_len;   // rows of 129..8192 entries given an ordered copy
+    unsigned long long ord_huge;  // rows above 8192 entries given an ordered copy
 };
 
 struct Graph {
@@ -163,6 +167,13 @@ struct Graph {
     uint32_t *big[2] = {nullptr, nullptr};   // h-index high-degree lists
     uint32_t *hx_bitmap = nullptr;           // h-index pending bitmap of odd sweeps (even: bitmap)
     HindexCtl *hctl = nullptr;
+    // h-index: rows above 128 entries copied in descending log2-degree buckets of the neighbours
+    uint32_t *hx_ord = nullptr;   // [nnz] (same positions as col; short rows unused)
+    uint32_t *hx_lid = nullptr;   // [n] index of a long row in hx_pref
+    uint32_t *hx_pref = nullptr;  // [32 per long row] entries in buckets >= b
+    uint8_t *hx_bk = nullptr;     // [nnz] bucket of each long-row entry (scratch of the copy)
+    uint8_t *hx_vb = nullptr;     // [n] floor(log2(degree)) of every vertex
+    uint64_t hx_ord_cap = 0, hx_lid_cap = 0, hx_pref_rows = 0;
     uint32_t *red = nullptr;          // small reduction scratch (min/max)
     // dynamic-graph maintenance
     uint32_t *mfront[2] = {nullptr, nullptr};

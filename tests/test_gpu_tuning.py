@@ -141,3 +141,67 @@ def test_hindex_warp_rows(warp_rows):
     got, _ = h.decompose("histo")
     assert np.array_equal(got, want)
     h.free()
+
+
+def _hub_graphs():
+    """Graphs whose long rows span many degree buckets: an R-MAT graph; a
+    400-clique plus a 29,600-leaf star (a hub above 4,096, so the CTA path
+    narrows its value range in sweep 0); a hub over 600 star centres of 600
+    leaves each (the centres start high and fall to 1, so the hub's estimate
+    falls by more than one histogram window); a hub joined to vertices of
+    degree 2^0 .. 2^13 and to a 300-clique."""
+    yield "rmat16", pg.rmat_graph(16, 16, seed=11)
+    k = 400
+    a, b = np.triu_indices(k, 1)
+    hub = np.arange(k, 30000, dtype=np.uint32)
+    yield "clique+star", pg.Graph.from_edges(np.concatenate([a, np.zeros(hub.size)]).astype(np.uint32),
+                                             np.concatenate([b, hub]).astype(np.uint32), 30000, dedup=True)
+    c = 600
+    centres = 1 + np.arange(c)
+    leaves = 1 + c + np.arange(c * c)
+    s = np.concatenate([np.zeros(c), np.repeat(centres, c)])
+    d = np.concatenate([centres, leaves])
+    yield "star-of-stars", pg.Graph.from_edges(s.astype(np.uint32), d.astype(np.uint32), 1 + c + c * c, dedup=True)
+    src, dst, nxt = [], [], 1
+    for e in range(14):  # neighbour nxt of the hub gets 2^e - 1 leaves of its own
+        src.append([0])
+        dst.append([nxt])
+        leaves = (1 << e) - 1
+        src.append(np.full(leaves, nxt))
+        dst.append(nxt + 1 + np.arange(leaves))
+        nxt += 1 + leaves
+    a, b = np.triu_indices(300, 1)
+    src += [a + nxt, np.zeros(300)]
+    dst += [b + nxt, nxt + np.arange(300)]
+    n = nxt + 300
+    yield "buckets", pg.Graph.from_edges(np.concatenate(src).astype(np.uint32), np.concatenate(dst).astype(np.uint32),
+                                         n, dedup=True)
+
+
+@pytest.mark.parametrize("order,order_min,warp_rows", [(1, 128, 8192), (1, 128, 512), (1, 128, 1 << 30),
+                                                       (1, 300, 8192), (1, 9000, 512), (0, 128, 8192)])
+def test_hindex_ordered_rows(order, order_min, warp_rows):
+    """Long rows read from the copy ordered by neighbour degree (prefix reads
+    in the support test, the bucket-by-bucket histogram and the notification
+    window), for the warp and CTA paths and with the copy limited to longer
+    rows or off: the same core numbers as Batagelj-Zaversnik, twice in a row
+    on the same graph."""
+    for name, g in _hub_graphs():
+        rp, col = g.csr()
+        want, _ = oracle.bz(rp, col)
+        g.set_param("hindex.order", order)
+        g.set_param("hindex.order_min", order_min)
+        g.set_param("hindex.warp_rows", warp_rows)
+        for method in ("histo", "nbr"):
+            got, _ = g.decompose(method)
+            assert np.array_equal(got, want), (name, method)
+        g.free()
+
+
+def test_hindex_order_min_range():
+    g = pg.rmat_graph(10, 8, seed=1)
+    for bad in (0, 127, (1 << 30) + 1):
+        with pytest.raises(pg.KCoreError):
+            g.set_param("hindex.order_min", bad)
+    g.set_param("hindex.order_min", 128)
+    g.free()
