@@ -15,7 +15,9 @@ Printed JSON line (rank 0):
              copies the CSR host->device (pinned), decomposes, copies the core
              array back and frees the graph; steps run from two host threads
              (independent graph handles), so one step's upload overlaps the
-             previous step's decomposition (serial_value: one thread);
+             previous step's decomposition (serial_value: one thread); the
+             same K steps as value, the pipeline's fill (the first upload,
+             which overlaps nothing) inside the timed region;
   roofline   algorithmic bytes B = 10*nnz + 16*n + 8 per decomposition over the
              main kernel's average CUDA-event duration, against the measured
              HBM copy bandwidth;
@@ -351,7 +353,7 @@ def run_engine(args, wl, world, rank, local, dist):
     ctypes.memmove(h_rp.value, rowptr.ctypes.data, 8 * (n + 1))
     ctypes.memmove(h_col.value, col.ctypes.data, 4 * nnz)
     core_view = np.ctypeslib.as_array((ctypes.c_uint32 * max(n, 1)).from_address(h_core.value))
-    e2e_steps = max(4, min(args.steps, 12))
+    e2e_steps = max(4, args.steps)
     mid = pg.method_id(method)
     depth = max(1, args.e2e_depth)
     h_cores = [h_core]
