@@ -168,14 +168,16 @@ __global__ void count_degrees(const uint32_t *__restrict__ src, const uint32_t *
     }
 }
 
+// cur: 64-bit row cursors preset to the row offsets, so one atomic gives an
+// entry's position with no row-offset read (random 8-byte reads of rowptr
+// were a third of this kernel's gathers: 8% of the C3 build measured).
 __global__ void scatter_edges(const uint32_t *__restrict__ src, const uint32_t *__restrict__ dst, uint64_t m,
-                              uint32_t n, const int64_t *__restrict__ rowptr, uint32_t *fill, uint32_t *col,
-                              uint32_t *key) {
+                              uint32_t n, unsigned long long *cur, uint32_t *col, uint32_t *key) {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < m; i += (uint64_t)gridDim.x * blockDim.x) {
         uint32_t a = src[i], b = dst[i];
         if (a >= n || b >= n || a == b) continue;
-        int64_t pa = rowptr[a] + atomicAdd(&fill[a], 1u);
-        int64_t pb = rowptr[b] + atomicAdd(&fill[b], 1u);
+        const unsigned long long pa = atomicAdd(&cur[a], 1ull);
+        const unsigned long long pb = atomicAdd(&cur[b], 1ull);
         col[pa] = b;
         col[pb] = a;
         if (key) {
@@ -671,9 +673,15 @@ int build_csr_from_edges(Graph *g, const uint32_t *d_src, const uint32_t *d_dst,
     rc = dalloc(&g->col, g->nnz + 1, "column ids");
     if (rc == KC_OK && keep_order) rc = dalloc(&key, g->nnz + 1, "edge order keys");
     if (rc) { dfree(deg); dfree(err); dfree(key); return rc; }
-    cudaMemsetAsync(deg, 0, ((uint64_t)n + 1) * 4, s);  // reused as fill cursors
-    if (m) scatter_edges<<<grid_for(m, 256, sms), 256, 0, s>>>(d_src, d_dst, m, n, g->rowptr, deg, g->col, key);
+    unsigned long long *cur = nullptr;  // row fill cursors, starting at the row offsets
+    if (m) {
+        rc = dalloc(&cur, (uint64_t)n + 1, "row cursors");
+        if (rc) { dfree(deg); dfree(err); dfree(key); return rc; }
+        cudaMemcpyAsync(cur, g->rowptr, ((uint64_t)n + 1) * 8, cudaMemcpyDeviceToDevice, s);
+        scatter_edges<<<grid_for(m, 256, sms), 256, 0, s>>>(d_src, d_dst, m, n, cur, g->col, key);
+    }
     e = cudaStreamSynchronize(s);
+    dfree(cur);
     if (e != cudaSuccess) { dfree(deg); dfree(err); dfree(key); return fail(KC_ERR_CUDA, "scatter: %s", cudaGetErrorString(e)); }
     if (keep_order) {
         rc = sort_rows(g, key, g->col, (uint32_t)(2 * m), s);
