@@ -206,20 +206,45 @@ __device__ __forceinline__ void hx_order_prefix(uint32_t *bins, uint32_t *pref_r
     bins[lane] = x - own;
 }
 
-// Ordered copies of the rows listed from the front of `rows` (up to
-// HX_ORD_WARP entries): one warp per row.  vb: the degree bucket of every
-// vertex.
-__global__ void __launch_bounds__(256) hx_order_warp(const int64_t *__restrict__ rowptr,
-                                                     const uint32_t *__restrict__ col,
-                                                     const uint8_t *__restrict__ vb, const uint32_t *rows,
-                                                     const HindexCtl *ctl, uint32_t *ord, uint32_t *pref,
-                                                     uint8_t *bk) {
-    __shared__ uint32_t sh[8][32];
+// Ordered copies of every listed row in one launch of 512-thread CTAs: each
+// CTA first takes rows above HX_ORD_WARP entries (listed from the far end of
+// `rows`, n entries) one at a time with all its warps, then its warps take
+// the shorter rows (listed from the front) one each, both from shared
+// cursors, so the long rows' tail overlaps the short rows.  vb: the degree
+// bucket of every vertex.
+constexpr int HX_ORD_THREADS = 512;
+__global__ void __launch_bounds__(HX_ORD_THREADS) hx_order_rows(const int64_t *__restrict__ rowptr,
+                                                                const uint32_t *__restrict__ col,
+                                                                const uint8_t *__restrict__ vb, const uint32_t *rows,
+                                                                uint32_t n, HindexCtl *ctl, uint32_t *ord,
+                                                                uint32_t *pref, uint8_t *bk, uint64_t max_long) {
+    constexpr int NW = HX_ORD_THREADS / 32;
+    __shared__ uint32_t cbins[32];
+    __shared__ uint32_t wbins[NW][32];
+    __shared__ unsigned long long item_sh;
     const unsigned lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const unsigned long long nrows = ctl->ord_len;
-    uint32_t *bins = sh[w];
-    for (unsigned long long i = (unsigned long long)blockIdx.x * 8 + w; i < nrows;
-         i += (unsigned long long)gridDim.x * 8) {
+    const unsigned long long nh = ctl->ord_huge, nrows = ctl->ord_len;
+    for (;;) {
+        if (threadIdx.x == 0) item_sh = atomicAdd(&ctl->ord_huge_cursor, 1ull);
+        if (threadIdx.x < 32) cbins[threadIdx.x] = 0;
+        __syncthreads();
+        const unsigned long long q = item_sh;
+        if (q >= nh) break;  // uniform: read after the barrier
+        const uint32_t v = rows[n - 1 - q];
+        const int64_t s = rowptr[v], e = rowptr[v + 1];
+        hx_order_count<NW>(col, vb, bk, s, e, cbins, w, lane);
+        __syncthreads();
+        if (w == 0) hx_order_prefix(cbins, pref + (max_long - 1 - q) * 32, lane);
+        __syncthreads();
+        hx_order_place<NW>(col, bk, s, e, cbins, ord, w, lane);
+        __syncthreads();
+    }
+    uint32_t *bins = wbins[w];
+    for (;;) {
+        unsigned long long i = 0;
+        if (lane == 0) i = atomicAdd(&ctl->ord_cursor, 1ull);
+        i = __shfl_sync(KC_FULL_MASK, i, 0);
+        if (i >= nrows) break;
         const uint32_t v = rows[i];
         const int64_t s = rowptr[v], e = rowptr[v + 1];
         bins[lane] = 0;
@@ -230,30 +255,6 @@ __global__ void __launch_bounds__(256) hx_order_warp(const int64_t *__restrict__
         __syncwarp();
         hx_order_place<1>(col, bk, s, e, bins, ord, 0, lane);
         __syncwarp();
-    }
-}
-
-// The rows above HX_ORD_WARP entries (listed from the far end of `rows`, n
-// entries): one CTA of 512 threads per row.
-__global__ void __launch_bounds__(512) hx_order_cta(const int64_t *__restrict__ rowptr,
-                                                    const uint32_t *__restrict__ col,
-                                                    const uint8_t *__restrict__ vb, const uint32_t *rows, uint32_t n,
-                                                    const HindexCtl *ctl, uint32_t *ord, uint32_t *pref,
-                                                    uint8_t *bk, uint64_t max_long) {
-    __shared__ uint32_t bins[32];
-    const unsigned lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const unsigned long long nh = ctl->ord_huge;
-    for (unsigned long long q = blockIdx.x; q < nh; q += gridDim.x) {
-        const uint32_t v = rows[n - 1 - q];
-        const int64_t s = rowptr[v], e = rowptr[v + 1];
-        if (threadIdx.x < 32) bins[threadIdx.x] = 0;
-        __syncthreads();
-        hx_order_count<16>(col, vb, bk, s, e, bins, w, lane);
-        __syncthreads();
-        if (w == 0) hx_order_prefix(bins, pref + (max_long - 1 - q) * 32, lane);
-        __syncthreads();
-        hx_order_place<16>(col, bk, s, e, bins, ord, w, lane);
-        __syncthreads();
     }
 }
 
@@ -1023,35 +1024,38 @@ static uint32_t order_min(const Graph *g) {
 }
 static uint64_t max_long_rows(const Graph *g) { return g->nnz / ((uint64_t)order_min(g) + 1) + 1; }
 
+static void free_hx_order(Graph *g) {
+    dfree(g->hx_ord);
+    dfree(g->hx_bk);
+    dfree(g->hx_lid);
+    dfree(g->hx_vb);
+    dfree(g->hx_pref);
+    g->hx_ord = g->hx_lid = g->hx_pref = nullptr;
+    g->hx_bk = g->hx_vb = nullptr;
+    g->hx_ord_cap = g->hx_lid_cap = g->hx_pref_rows = 0;
+}
+
+// The buffers of the ordered copy, kept for later decompositions of the same
+// graph (regrown when an update enlarged it); on a failed allocation all are
+// released, so that a decomposition without the copy has the memory.
 static int ensure_hx_order(Graph *g) {
-    if (!g->hx_ord || !g->hx_bk || g->hx_ord_cap < g->nnz) {
-        dfree(g->hx_ord);
-        g->hx_ord = nullptr;
-        g->hx_ord_cap = 0;
-        dfree(g->hx_bk);
-        g->hx_bk = nullptr;
-        KC_TRY(dalloc(&g->hx_ord, g->nnz + 1, "h-index ordered rows"));
-        KC_TRY(dalloc(&g->hx_bk, g->nnz + 1, "h-index entry buckets"));
-        g->hx_ord_cap = g->nnz;
-    }
-    if (!g->hx_lid || !g->hx_vb || g->hx_lid_cap < g->n) {
-        dfree(g->hx_lid);
-        g->hx_lid = nullptr;
-        g->hx_lid_cap = 0;
-        dfree(g->hx_vb);
-        g->hx_vb = nullptr;
-        KC_TRY(dalloc(&g->hx_lid, (uint64_t)g->n + 1, "h-index long-row index"));
-        KC_TRY(dalloc(&g->hx_vb, (uint64_t)g->n + 1, "h-index degree buckets"));
-        g->hx_lid_cap = g->n;
-    }
     const uint64_t rows = max_long_rows(g);
-    if (!g->hx_pref || g->hx_pref_rows < rows) {
-        dfree(g->hx_pref);
-        g->hx_pref = nullptr;
-        g->hx_pref_rows = 0;
-        KC_TRY(dalloc(&g->hx_pref, rows * 32, "h-index bucket prefixes"));
-        g->hx_pref_rows = rows;
+    if (g->hx_ord && g->hx_bk && g->hx_ord_cap >= g->nnz && g->hx_lid && g->hx_vb && g->hx_lid_cap >= g->n &&
+        g->hx_pref && g->hx_pref_rows >= rows)
+        return KC_OK;
+    free_hx_order(g);
+    int rc = dalloc(&g->hx_ord, g->nnz + 1, "h-index ordered rows");
+    if (!rc) rc = dalloc(&g->hx_bk, g->nnz + 1, "h-index entry buckets");
+    if (!rc) rc = dalloc(&g->hx_lid, (uint64_t)g->n + 1, "h-index long-row index");
+    if (!rc) rc = dalloc(&g->hx_vb, (uint64_t)g->n + 1, "h-index degree buckets");
+    if (!rc) rc = dalloc(&g->hx_pref, rows * 32, "h-index bucket prefixes");
+    if (rc) {
+        free_hx_order(g);
+        return rc;
     }
+    g->hx_ord_cap = g->nnz;
+    g->hx_lid_cap = g->n;
+    g->hx_pref_rows = rows;
     return KC_OK;
 }
 
@@ -1129,8 +1133,18 @@ static int ensure_events(Graph *g) {
 int hindex_run(Graph *g, cudaStream_t s, kc_stats *st) {
     KC_TRY(ensure_hx_buffers(g));
     KC_TRY(ensure_events(g));
-    const bool ordered = g->tune.hindex_order && g->nnz > 0;
-    if (ordered) KC_TRY(ensure_hx_order(g));
+    bool ordered = g->tune.hindex_order && g->nnz > 0;
+    if (ordered) {
+        // without room for the copy (5 bytes per entry and a table), the
+        // iteration reads the rows as they are
+        const int rc = ensure_hx_order(g);
+        if (rc == KC_ERR_NOMEM) {
+            clear_error();
+            ordered = false;
+        } else if (rc) {
+            return rc;
+        }
+    }
     KC_CUDA(cudaEventRecord(g->ev0, s));
     KC_CUDA(cudaMemsetAsync(g->hctl, 0, sizeof(HindexCtl), s));
     const int ig = std::max(1, std::min<int>(g->sm_count * 8, (int)((g->n + 255) / 256)));
@@ -1139,12 +1153,10 @@ int hindex_run(Graph *g, cudaStream_t s, kc_stats *st) {
     hindex_init<<<ig, 256, 0, s>>>(g->rowptr, g->n, g->core, g->bitmap, g->hx_bitmap, g->big[0],
                                    ordered ? g->list[1] : nullptr, g->hx_lid, ordered ? g->hx_vb : nullptr,
                                    order_min(g), max_long_rows(g), g->hctl);
-    if (ordered) {
-        hx_order_warp<<<g->sm_count * 8, 256, 0, s>>>(g->rowptr, g->col, g->hx_vb, g->list[1], g->hctl, g->hx_ord,
-                                                      g->hx_pref, g->hx_bk);
-        hx_order_cta<<<g->sm_count * 2, 512, 0, s>>>(g->rowptr, g->col, g->hx_vb, g->list[1], g->n, g->hctl,
-                                                     g->hx_ord, g->hx_pref, g->hx_bk, max_long_rows(g));
-    }
+    if (ordered)
+        hx_order_rows<<<g->sm_count * 4, HX_ORD_THREADS, 0, s>>>(g->rowptr, g->col, g->hx_vb, g->list[1], g->n,
+                                                                 g->hctl, g->hx_ord, g->hx_pref, g->hx_bk,
+                                                                 max_long_rows(g));
     return hindex_launch(g, s, st, true, ordered);
 }
 

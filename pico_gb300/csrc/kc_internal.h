@@ -134,6 +134,7 @@ struct HindexCtl {
     unsigned int err_info;
     unsigned long long ord_len;   // rows of 129..8192 entries given an ordered copy
     unsigned long long ord_huge;  // rows above 8192 entries given an ordered copy
+    unsigned long long ord_cursor, ord_huge_cursor;  // work cursors of the copy
 };
 
 struct Graph {
