@@ -278,6 +278,8 @@ def run_engine(args, wl, world, rank, local, dist):
     device = local
     torch.cuda.set_device(device)
     g = make_graph(pg, wl, device)
+    for name, val in args.param:
+        g.set_param(name, val)
     n, nnz = g.n, g.nnz
     m = nnz // 2
     stream = torch.cuda.Stream(device=device)
@@ -319,7 +321,8 @@ def run_engine(args, wl, world, rank, local, dist):
     achieved = bytes_alg / (kavg / 1e3) / 1e9
     peak, peak_kind = load_peaks()
     kernel_name = "hindex_kernel" if pg.method_id(method) in (0, 1, 2) else "peel_kernel"
-    traffic = load_traffic(kernel_name, args.workload)
+    # the recorded traffic belongs to the default tunables
+    traffic = None if args.param else load_traffic(kernel_name, args.workload)
 
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "M edges/s", "n_gpus": world,
@@ -330,7 +333,7 @@ def run_engine(args, wl, world, rank, local, dist):
                    "parallelism": "replicas x%d (graph does not shard)" % world,
                    "l2": "inputs larger than L2 (col array %.0f MB > 129 MB L2)" % (4 * nnz / 1e6),
                    "kmax": st.kmax, "levels": st.levels, "level_indices": st.iterations,
-                   "build_ms": round(st.build_ms, 3)},
+                   "build_ms": round(st.build_ms, 3), **({"params": dict(args.param)} if args.param else {})},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic, "peak_kind": peak_kind,
                      "kernel": kernel_name, "bytes_per_launch": bytes_alg,
@@ -371,6 +374,8 @@ def run_engine(args, wl, world, rank, local, dist):
         out = free_cores.get()
         try:
             h = pg.Graph.from_csr_ptr(h_rp.value, h_col.value, n, device=device)
+            for name, val in args.param:
+                h.set_param(name, val)
             pg.check(pg.lib().kc_decompose(h.handle, mid, pg.ctypes.c_void_p(out.value), 0, None, None))
             h.free()
         finally:
@@ -843,6 +848,13 @@ def serve_exact(base_rowptr, base_col, reqs, results):
     return all(ok), len(ok)
 
 
+def _param(text):
+    name, sep, value = text.partition("=")
+    if not sep or not name:
+        raise argparse.ArgumentTypeError("expected NAME=VALUE, got %r" % text)
+    return name, int(value, 0)
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -851,6 +863,9 @@ def main():
     ap.add_argument("--impl", choices=["engine", "reference"], default="engine")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="rmat25planted")
     ap.add_argument("--method", default="peelone_dyn")
+    ap.add_argument("--param", action="append", default=[], type=_param, metavar="NAME=VALUE",
+                    help="a kc_graph_set_param tunable applied to the main graph (repeatable; the "
+                         "roofline's traffic figure is then left out)")
     ap.add_argument("--clock-window", type=float, default=1.5,
                     help="seconds of identical load before the timed steps, so clocks are sampled under load")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
