@@ -22,8 +22,9 @@
 //   * otherwise the h-index comes from a degree-capped histogram built in
 //     shared memory and a suffix scan: 8 lanes per vertex for rows of at
 //     most 32 entries, one warp per vertex for rows of at most 8,192 entries
-//     (512 in sweep 0, where estimates are still degrees), with a window of
-//     512 values below the estimate; otherwise one CTA,
+//     (512 in sweep 0, where estimates are still degrees, unless the rows are
+//     ordered: see below), with a window of 512 values below the estimate;
+//     otherwise one CTA,
 //     which narrows the value range with 4096-bin passes until bins are one
 //     value wide;
 //   * rows above 128 entries are read from a copy made at the start of the
@@ -34,7 +35,11 @@
 //     degree >= c[v], the notification those of degree > the new estimate,
 //     and the histogram grows one bucket at a time until the h-index is
 //     pinned (count(>= k) is exact for every k at or above the last bucket
-//     read).  On R-MAT graphs this reads about 40% fewer row entries;
+//     read).  The prefix lengths alone also bound the h-index (no k above
+//     P[floor(log2 k)] qualifies); when the bound is below the estimate the
+//     support test is skipped and the histogram window is put under the
+//     bound, so sweep 0 gives rows up to 8,192 entries to warps.  On R-MAT
+//     graphs this reads about 40% fewer row entries;
 //   * updates are visible at once within a sweep (Gauss-Seidel), which only
 //     shortens the trajectory; sweeps are separated by a grid barrier with a
 //     bounded wait.
@@ -73,21 +78,22 @@ struct HxArgs {
     uint32_t first_all;  // sweep 0 covers every vertex (else list[0] / big[0])
     uint32_t withhold;   // CTA 0 never arrives at the first barrier (failure-detection hook)
     uint32_t warp_rows;  // rows up to this length are re-examined by one warp
+    uint32_t sweep0_rows;  // in sweep 0: HX_WARP_MAX, or warp_rows when long rows are ordered
     PeelTrace *trace;    // per-sweep trace or nullptr
     uint32_t trace_cap;
 };
 
 __device__ __forceinline__ unsigned hx_bucket(uint32_t x) { return x ? 31u - __clz(x) : 0u; }
 
-// Estimates start at the degrees; rows above HX_WARP_MAX entries are queued
+// Estimates start at the degrees; rows above sweep0_rows entries are queued
 // for the CTAs of sweep 0.  With ord_rows, the rows above ord_min entries
 // are listed for the ordered copy: up to HX_ORD_WARP entries from the front
 // of ord_rows (long-row index p), longer ones from its far end (index
 // max_long - 1 - q), each with its index in lid, and vb holds every
 // vertex's degree bucket (one byte: the copies gather these, not degrees).
 __global__ void hindex_init(const int64_t *__restrict__ rowptr, uint32_t n, uint32_t *c, uint32_t *inlist0,
-                            uint32_t *inlist1, uint32_t *big0, uint32_t *ord_rows, uint32_t *lid, uint8_t *vb,
-                            uint32_t ord_min, uint64_t max_long, HindexCtl *ctl) {
+                            uint32_t *inlist1, uint32_t *big0, uint32_t sweep0_rows, uint32_t *ord_rows,
+                            uint32_t *lid, uint8_t *vb, uint32_t ord_min, uint64_t max_long, HindexCtl *ctl) {
     const unsigned lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
@@ -98,7 +104,7 @@ __global__ void hindex_init(const int64_t *__restrict__ rowptr, uint32_t n, uint
             uint32_t d = (uint32_t)(rowptr[v + 1] - rowptr[v]);
             c[v] = d;
             if (vb) vb[v] = (uint8_t)hx_bucket(d);
-            bigv = d > HX_WARP_MAX;
+            bigv = d > sweep0_rows;
             midl = ord_rows && d > ord_min && d <= HX_ORD_WARP;
             hugel = ord_rows && d > ord_min && d > HX_ORD_WARP;
         }
@@ -379,6 +385,17 @@ struct HxRow {
         const uint32_t p = __shfl_sync(KC_FULL_MASK, pf, t ? 31 - __clz(t) : 0);
         return ordered && t ? s + (int64_t)p : e;
     }
+    // An upper bound of the h-index from the prefix lengths alone (ordered
+    // rows): count(>= k) <= P[floor(log2 k)], so no k in a bucket b with
+    // P[b] < 2^b qualifies, and k <= P[b] for the highest bucket b that can.
+    __device__ __forceinline__ uint32_t hbound() const {
+        const unsigned lane = threadIdx.x & 31;
+        const unsigned ok = __ballot_sync(KC_FULL_MASK, pf >= (1u << lane));
+        if (!ok) return 0;
+        const unsigned b = 31 - __clz(ok);
+        const uint32_t pb = __shfl_sync(KC_FULL_MASK, pf, b);
+        return b >= 31 ? pb : min(pb, (2u << b) - 1u);
+    }
 };
 
 // The h-index lies below lo (above = count(>= lo)): windows of HX_WARP_MAX
@@ -460,7 +477,8 @@ __device__ bool hx_warp_vertex(const HxArgs &A, uint32_t v, unsigned cur, bool c
     R.pf = R.ordered ? A.pref[(size_t)A.lid[v] * 32 + lane] : 0u;
     uint32_t cu[HX_CACHE], cv[HX_CACHE];
     uint32_t cnt = 0;
-    uint32_t lo = 0;  // lowest value the histogram window covers
+    uint32_t lo = 0;      // lowest value the histogram window covers
+    uint32_t capw = cap;  // its top bin counts the values at or above capw
     if (cached) {
 #pragma unroll
         for (int k = 0; k < HX_CACHE; k++) {
@@ -480,16 +498,23 @@ __device__ bool hx_warp_vertex(const HxArgs &A, uint32_t v, unsigned cur, bool c
         for (int k = 0; k < HX_CACHE; k++)
             if (cu[k] != 0xffffffffu) atomicAdd(&hist[cv[k] < cap ? cv[k] : cap], 1u);
     } else {
-        // One pass counts the values at or above cap and builds the histogram
-        // of those in the window [lo, cap) of at most HX_WARP_MAX values (bin
-        // x - lo); it stops early once the support test holds.  An ordered
-        // row is read only as far as the neighbours of degree >= cap.
-        lo = cap > HX_WARP_MAX ? cap - HX_WARP_MAX : 0u;
-        for (uint32_t b = lane; b < cap - lo; b += 32) hist[b] = 0;
+        // One pass counts the values at or above capw and builds the
+        // histogram of those in the window [lo, capw) of at most HX_WARP_MAX
+        // values (bin x - lo); it stops early once the support test holds.
+        // An ordered row is read only as far as the neighbours of degree >=
+        // capw, and capw is lowered to one above the row's h-index bound:
+        // below cap, the support test cannot hold (the common case in sweep 0,
+        // where estimates are still degrees).
+        if (R.ordered) {
+            const uint32_t hb = R.hbound();
+            if (hb < cap) capw = hb + 1;
+        }
+        lo = capw > HX_WARP_MAX ? capw - HX_WARP_MAX : 0u;
+        for (uint32_t b = lane; b < capw - lo; b += 32) hist[b] = 0;
         __syncwarp();
-        cnt = hx_warp_gather(R.r, A.c, s, R.end(cap), hist, lo, cap, 0u, cap, lane);
-        if (cnt >= cap) return false;  // support intact: estimate stands
-        if (lane == 0) hist[cap - lo] = cnt;
+        cnt = hx_warp_gather(R.r, A.c, s, R.end(capw), hist, lo, capw, 0u, capw == cap ? cap : 0u, lane);
+        if (capw == cap && cnt >= cap) return false;  // support intact: estimate stands
+        if (lane == 0) hist[capw - lo] = cnt;
     }
     __syncwarp();
     // Suffix scan of the window from its top bin: the largest k with
@@ -498,12 +523,12 @@ __device__ bool hx_warp_vertex(const HxArgs &A, uint32_t v, unsigned cur, bool c
     uint32_t carry = 0;
     int64_t hk;
     if (!R.ordered) {
-        hk = hx_warp_scan(hist, lo, cap, lane, carry);
+        hk = hx_warp_scan(hist, lo, capw, lane, carry);
     } else {
         // all buckets >= b are in the histogram, so count(>= k) is exact for
         // k >= 2^b: scan down to there, then add the next bucket
-        unsigned b = hx_bucket(cap);
-        int64_t top = cap, jr = R.end(cap);
+        unsigned b = hx_bucket(capw);
+        int64_t top = capw, jr = R.end(capw);
         for (;;) {
             const uint32_t kmin = max(max(1u << b, lo), 1u);
             hk = hx_warp_scan_from(hist, lo, top, kmin, lane, carry);
@@ -511,7 +536,7 @@ __device__ bool hx_warp_vertex(const HxArgs &A, uint32_t v, unsigned cur, bool c
             top = (int64_t)kmin - 1;
             b--;
             const int64_t j1 = R.end(1u << b);
-            hx_warp_gather(R.r, A.c, jr, j1, hist, lo, cap, 0u, 0u, lane);
+            hx_warp_gather(R.r, A.c, jr, j1, hist, lo, capw, 0u, 0u, lane);
             jr = j1;
             __syncwarp();
         }
@@ -718,18 +743,28 @@ __device__ bool hx_block_vertex(const HxArgs &A, uint32_t v, unsigned nxt, uint3
     auto upto = [&](uint32_t t) -> int64_t { return ordered && t ? s + (int64_t)pref_sh[hx_bucket(t)] : e; };
     const uint32_t cap = cap_sh;
     if (cap == 0) return false;
+    // capw: one above the h-index bound of an ordered row (see HxRow::hbound),
+    // if that is below cap (then the support test cannot hold), else cap
+    uint32_t capw = cap;
+    if (ordered) {
+        int b = 31;
+        while (b > 0 && pref_sh[b] < (1u << b)) b--;
+        const uint32_t hb = b >= 31 ? pref_sh[b] : min(pref_sh[b], (2u << b) - 1u);
+        if (hb < cap) capw = hb + 1;
+    }
     // Support test in chunks that double from 2,048 entries; it stops as
-    // soon as cap neighbours at >= cap have been seen.  For cap <= HX_BINS
-    // the same pass builds the histogram of the values below cap.
-    const bool onepass = cap <= HX_BINS;
+    // soon as cap neighbours at >= cap have been seen.  For capw <= HX_BINS
+    // the same pass builds the histogram of the values below capw.
+    const bool onepass = capw <= HX_BINS;
     if (onepass) {
-        for (uint32_t b = threadIdx.x; b < cap; b += HX_THREADS) hist[b] = 0;
+        for (uint32_t b = threadIdx.x; b < capw; b += HX_THREADS) hist[b] = 0;
         __syncthreads();
     }
-    uint32_t cnt = 0;
+    uint32_t cnt = 0;  // values at or above capw
     int64_t span = 4 * HX_THREADS;
-    const int64_t e1 = upto(cap);
-    for (int64_t j0 = s; j0 < e1 && cnt < cap; span *= 2) {
+    const int64_t e1 = upto(capw);
+    const uint32_t stop = capw == cap ? cap : 0xffffffffu;
+    for (int64_t j0 = s; j0 < e1 && cnt < stop; span *= 2) {
         const int64_t j1 = e1 - j0 < span ? e1 : j0 + span;
         uint32_t c1 = 0;
         for (int64_t jb = j0 + threadIdx.x; jb < j1; jb += HX_CACHE * HX_THREADS) {
@@ -744,26 +779,26 @@ __device__ bool hx_block_vertex(const HxArgs &A, uint32_t v, unsigned nxt, uint3
 #pragma unroll
             for (int k = 0; k < HX_CACHE; k++)
                 if (uu[k] != 0xffffffffu) {
-                    if (xx[k] >= cap) c1++;
+                    if (xx[k] >= capw) c1++;
                     else if (onepass) atomicAdd(&hist[xx[k]], 1u);
                 }
         }
         cnt += block_sum(c1, red);
         j0 = j1;
     }
-    if (cnt >= cap) return false;
+    if (capw == cap && cnt >= cap) return false;
     uint32_t h = 0;
     if (onepass && !ordered) {
-        const int b = hx_block_suffix_find(hist, (int)cap, 0, 1, cnt, red);
+        const int b = hx_block_suffix_find(hist, (int)capw, 0, 1, cnt, red);
         h = b < 0 ? 0u : (uint32_t)b;
     } else if (onepass) {
         // every bucket >= b is in the histogram, so count(>= k) is exact for
         // k >= 2^b: look for the h-index there, else add the next bucket
-        unsigned b = hx_bucket(cap);
+        unsigned b = hx_bucket(capw);
         int64_t jr = e1;
         for (;;) {
             const uint32_t kmin = 1u << b;
-            const int r = hx_block_suffix_find(hist + kmin, (int)(cap - kmin), kmin, 1, cnt, red);
+            const int r = hx_block_suffix_find(hist + kmin, (int)(capw - kmin), kmin, 1, cnt, red);
             if (r >= 0) {
                 h = kmin + (uint32_t)r;
                 break;
@@ -782,7 +817,7 @@ __device__ bool hx_block_vertex(const HxArgs &A, uint32_t v, unsigned nxt, uint3
                 for (int k = 0; k < HX_CACHE; k++) xx[k] = uu[k] != 0xffffffffu ? __ldcg(&A.c[uu[k]]) : 0u;
 #pragma unroll
                 for (int k = 0; k < HX_CACHE; k++)
-                    if (uu[k] != 0xffffffffu && xx[k] < cap) atomicAdd(&hist[xx[k]], 1u);
+                    if (uu[k] != 0xffffffffu && xx[k] < capw) atomicAdd(&hist[xx[k]], 1u);
             }
             jr = j1;
             __syncthreads();
@@ -791,7 +826,7 @@ __device__ bool hx_block_vertex(const HxArgs &A, uint32_t v, unsigned nxt, uint3
         // narrow [lo, hi) -- known to contain h -- with 4096-bin passes until
         // the bins are one value wide; `above` counts neighbours at >= hi.
         // A pass reads the part of the row that can hold values >= lo.
-        uint64_t lo = 0, hi = cap;
+        uint64_t lo = 0, hi = capw;
         for (;;) {
             const uint64_t w = (hi - lo + HX_BINS - 1) / HX_BINS;
             const int nb = (int)((hi - lo + w - 1) / w);
@@ -931,14 +966,14 @@ __global__ void __launch_bounds__(HX_THREADS, 2) hindex_kernel(HxArgs A) {
             const unsigned cntv = (unsigned)(nsmall - base < HX_GRAB ? nsmall - base : HX_GRAB);
             // the grab's vertices and row lengths on lanes 0..cntv-1; rows
             // of at most HX_TINY entries go four at a time, the others one
-            // per warp (sweep 0 leaves rows above HX_WARP_MAX to the CTAs)
+            // per warp (sweep 0 leaves rows above A.sweep0_rows to the CTAs)
             uint32_t vi = 0;
             int64_t di = 0;
             if (lane < cntv) {
                 vi = all ? (uint32_t)(base + lane) : A.list[cur][base + lane];
                 di = A.rowptr[vi + 1] - A.rowptr[vi];
             }
-            const bool in = lane < cntv && !(all && di > (int64_t)HX_WARP_MAX);
+            const bool in = lane < cntv && !(all && di > (int64_t)A.sweep0_rows);
             unsigned tinym = __ballot_sync(KC_FULL_MASK, in && di <= (int64_t)HX_TINY);
             unsigned restm = __ballot_sync(KC_FULL_MASK, in && di > (int64_t)HX_TINY);
             while (tinym) {
@@ -1024,6 +1059,14 @@ static uint32_t order_min(const Graph *g) {
 }
 static uint64_t max_long_rows(const Graph *g) { return g->nnz / ((uint64_t)order_min(g) + 1) + 1; }
 
+// Rows up to this length are evaluated by one warp in sweep 0, where the
+// estimates are still degrees: a warp's 512-value window below the estimate
+// misses the h-index of a longer row unless the row is ordered (its prefix
+// lengths bound the h-index, and the window is put below that bound).
+static uint32_t sweep0_rows(const Graph *g, bool ordered) {
+    return ordered && order_min(g) <= HX_WARP_MAX ? (uint32_t)g->tune.hindex_warp_rows : HX_WARP_MAX;
+}
+
 static void free_hx_order(Graph *g) {
     dfree(g->hx_ord);
     dfree(g->hx_bk);
@@ -1090,6 +1133,7 @@ static int hindex_launch(Graph *g, cudaStream_t s, kc_stats *st, bool first_all,
     A.max_sweeps = (uint32_t)std::min<uint64_t>(2 * ((uint64_t)g->nnz + 1) + 4, 0xffffffffull);
     A.first_all = first_all ? 1u : 0u;
     A.warp_rows = (uint32_t)g->tune.hindex_warp_rows;
+    A.sweep0_rows = sweep0_rows(g, ordered);
     A.trace = g->tune.trace ? g->trace : nullptr;
     A.trace_cap = g->tune.trace ? g->trace_cap : 0;
     if (A.trace) KC_CUDA(cudaMemsetAsync(g->trace, 0, sizeof(PeelTrace) * g->trace_cap, s));
@@ -1151,8 +1195,8 @@ int hindex_run(Graph *g, cudaStream_t s, kc_stats *st) {
     // the ordered copies of the long rows (part of every decomposition's
     // time); list[1] holds the rows to copy until sweep 0 queues vertices there
     hindex_init<<<ig, 256, 0, s>>>(g->rowptr, g->n, g->core, g->bitmap, g->hx_bitmap, g->big[0],
-                                   ordered ? g->list[1] : nullptr, g->hx_lid, ordered ? g->hx_vb : nullptr,
-                                   order_min(g), max_long_rows(g), g->hctl);
+                                   sweep0_rows(g, ordered), ordered ? g->list[1] : nullptr, g->hx_lid,
+                                   ordered ? g->hx_vb : nullptr, order_min(g), max_long_rows(g), g->hctl);
     if (ordered)
         hx_order_rows<<<g->sm_count * 4, HX_ORD_THREADS, 0, s>>>(g->rowptr, g->col, g->hx_vb, g->list[1], g->n,
                                                                  g->hctl, g->hx_ord, g->hx_pref, g->hx_bk,

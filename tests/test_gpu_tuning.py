@@ -83,22 +83,24 @@ def test_trace_records_levels():
 
 def test_trace_records_hindex_sweeps():
     """After an h-index decomposition the trace holds one record per sweep:
-    sweep 0 examines every vertex (short rows by warps, rows above 512
-    entries by CTAs), the last sweep lowers nothing, and the estimates
-    lowered add up to at least the total drop from degree to core number in
-    steps of one vertex each."""
+    sweep 0 examines every vertex (short rows by warps; by CTAs the rows
+    above 8,192 entries, or above 512 without the degree-ordered copy of the
+    long rows), the last sweep lowers nothing, and the estimates lowered add
+    up to at least the total drop from degree to core number in steps of one
+    vertex each."""
     g = pg.rmat_graph(16, 16, seed=7)
     rp, col = g.csr()
     deg = np.diff(rp)
-    g.set_param("trace", 1)
-    core, st = g.decompose("histo")
     want, _ = oracle.bz(rp, col)
-    assert np.array_equal(core, want)
-    tr = g.trace()
-    assert len(tr) == st.iterations >= 2
-    assert [r["level"] for r in tr] == list(range(len(tr)))
-    long_rows = int((deg > 512).sum())
-    assert tr[0]["spilled"] == long_rows and tr[0]["scan_len"] == g.n
+    g.set_param("trace", 1)
+    for order, cta_rows in ((0, 512), (1, 8192)):
+        g.set_param("hindex.order", order)
+        core, st = g.decompose("histo")
+        assert np.array_equal(core, want)
+        tr = g.trace()
+        assert len(tr) == st.iterations >= 2
+        assert [r["level"] for r in tr] == list(range(len(tr)))
+        assert tr[0]["spilled"] == int((deg > cta_rows).sum()) and tr[0]["scan_len"] == g.n
     assert tr[-1]["claimed"] == 0
     lowered = sum(r["claimed"] for r in tr)
     assert lowered >= int((core < deg).sum())
