@@ -228,7 +228,9 @@ int kc_graph_last_timing(const kc_graph *g, double *total_ms, double *kernel_ms)
  * at least 128),
  * "trace" (1 = record a per-level trace of the next decompositions),
  * "update.incremental_max" (largest update batch, in edges, maintained
- * incrementally by kc_graph_update), "wait.timeout_us" (limit of one
+ * incrementally by kc_graph_update; default 512),
+ * "update.deletion_incremental_max" (the same for batches of deletions only;
+ * default 500,000), "wait.timeout_us" (limit of one
  * inter-CTA wait of the peel and h-index kernels, default 2 s; a wait that
  * runs out makes the call return KC_ERR_TIMEOUT), "test.withhold" (1 = one
  * CTA never signals the others, so their waits run out: exercises the
@@ -278,7 +280,8 @@ int kc_graph_kcore_subgraph(const kc_graph *g, uint32_t k, kc_graph **out, uint3
  * KC_EDGES_DEDUP (sorted rows, no parallel edges) and keeps the core numbers
  * exact: deletions first, then insertions; deleting an absent edge or
  * inserting a present one is ignored; self-loops are ignored.  Batches of at
- * most "update.incremental_max" edges (kc_graph_set_param) are maintained
+ * most "update.incremental_max" edges (kc_graph_set_param), and batches of
+ * deletions only up to "update.deletion_incremental_max" edges, are maintained
  * incrementally (h-index iteration from the old cores for deletions;
  * matching rounds with subcore candidate sets for insertions); larger ones
  * are applied in one rewrite followed by a full decomposition.  Edge lists in

@@ -677,6 +677,9 @@ int kc_graph_set_param(kc_graph *g, const char *name, int64_t value) {
     } else if (k == "update.incremental_max") {
         if (value < 0) return fail(KC_ERR_INVALID, "update.incremental_max: >= 0");
         t.update_incremental_max = value;
+    } else if (k == "update.deletion_incremental_max") {
+        if (value < 0) return fail(KC_ERR_INVALID, "update.deletion_incremental_max: >= 0");
+        t.update_deletion_incremental_max = value;
     } else if (k == "wait.timeout_us") {
         if (value < 1000 || value > 600000000) return fail(KC_ERR_INVALID, "wait.timeout_us: [1000, 6e8]");
         t.wait_timeout_us = value;

@@ -491,12 +491,16 @@ __device__ bool hx_warp_vertex(const HxArgs &A, uint32_t v, unsigned cur, bool c
         for (int k = 0; k < HX_CACHE; k++) cnt += (cu[k] != 0xffffffffu && cv[k] >= cap) ? 1u : 0u;
         cnt = __reduce_add_sync(KC_FULL_MASK, cnt);
         if (cnt >= cap) return false;  // support intact: estimate stands
-        // histogram of min(c[u], cap) over bins [0, cap]; cap <= degree <= 128
-        for (uint32_t b = lane; b <= cap; b += 32) hist[b] = 0;
+        // histogram of min(c[u], capw) over bins [0, capw], capw = min(cap,
+        // row length) <= 128: the h-index is at most the row length, and an
+        // estimate above it (an old core number after deletions) still
+        // decides the notification window below
+        capw = min(cap, (uint32_t)(e - s));
+        for (uint32_t b = lane; b <= capw; b += 32) hist[b] = 0;
         __syncwarp();
 #pragma unroll
         for (int k = 0; k < HX_CACHE; k++)
-            if (cu[k] != 0xffffffffu) atomicAdd(&hist[cv[k] < cap ? cv[k] : cap], 1u);
+            if (cu[k] != 0xffffffffu) atomicAdd(&hist[cv[k] < capw ? cv[k] : capw], 1u);
     } else {
         // One pass counts the values at or above capw and builds the
         // histogram of those in the window [lo, capw) of at most HX_WARP_MAX
@@ -615,22 +619,24 @@ __device__ unsigned hx_warp_tiny(const HxArgs &A, uint32_t vg, bool valid, unsig
     cnt += __shfl_xor_sync(KC_FULL_MASK, cnt, 2);
     cnt += __shfl_xor_sync(KC_FULL_MASK, cnt, 4);
     const bool act = valid && cap > 0 && cnt < cap;  // the same on the group's lanes
+    // bins [0, capt], capt = min(cap, row length) <= HX_TINY (see hx_warp_vertex)
+    const uint32_t capt = min(cap, (uint32_t)(e - s));
     uint32_t *hb = hist + gi * (HX_TINY + 1);
     if (act)
-        for (uint32_t b = gl; b <= cap; b += 8) hb[b] = 0;
+        for (uint32_t b = gl; b <= capt; b += 8) hb[b] = 0;
     __syncwarp();
     if (act) {
 #pragma unroll
         for (int k = 0; k < 4; k++)
-            if (cu[k] != 0xffffffffu) atomicAdd(&hb[cv[k] < cap ? cv[k] : cap], 1u);
+            if (cu[k] != 0xffffffffu) atomicAdd(&hb[cv[k] < capt ? cv[k] : capt], 1u);
     }
     __syncwarp();
-    // lane gl holds bins cap - 4 gl - t (t = 0..3, from the top): suffix
+    // lane gl holds bins capt - 4 gl - t (t = 0..3, from the top): suffix
     // counts from the bins of the lanes before it, then its own
     uint32_t loc[4], lsum = 0;
 #pragma unroll
     for (int t = 0; t < 4; t++) {
-        const int k = (int)cap - 4 * (int)gl - t;
+        const int k = (int)capt - 4 * (int)gl - t;
         loc[t] = act && k >= 1 ? hb[k] : 0u;
         lsum += loc[t];
     }
@@ -644,7 +650,7 @@ __device__ unsigned hx_warp_tiny(const HxArgs &A, uint32_t vg, bool valid, unsig
     int best = 0;  // the largest k with count(>= k) >= k (0 if none)
 #pragma unroll
     for (int t = 0; t < 4; t++) {
-        const int k = (int)cap - 4 * (int)gl - t;
+        const int k = (int)capt - 4 * (int)gl - t;
         run += loc[t];
         if (act && k >= 1 && run >= (uint32_t)k && best == 0) best = k;
     }
@@ -1218,8 +1224,9 @@ __global__ void hindex_seed(const int64_t *__restrict__ rowptr, const uint32_t *
 }
 
 // h-index iteration from the current contents of g->core (which must be
-// upper bounds of the core numbers), starting with the vertices of d_list
-// active.  Used by the maintenance of dynamic graphs.
+// upper bounds of the core numbers; after deletions they can exceed a
+// vertex's degree), starting with the vertices of d_list active.  Used by the
+// maintenance of dynamic graphs.
 int hindex_run_from(Graph *g, const uint32_t *d_list, uint64_t len, cudaStream_t s, kc_stats *st) {
     KC_TRY(ensure_hx_buffers(g));
     KC_TRY(ensure_events(g));

@@ -113,6 +113,7 @@ struct Tuning {
     int hindex_order = 1;  // h-index: long rows read from a copy ordered by neighbour degree (prefix reads)
     int64_t hindex_order_min = 128;  // h-index: rows above this length get the ordered copy
     int64_t update_incremental_max = 512;  // larger update batches: full recompute (measured crossover ~1000 edges)
+    int64_t update_deletion_incremental_max = 500000;  // deletion-only batches (crossover ~600,000 on R-MAT 22)
     int64_t wait_timeout_us = 2000000;       // limit of one inter-CTA wait
     int withhold = 0;  // failure-detection hook: one CTA never signals, so the others' waits run out
 };

@@ -18,8 +18,9 @@
 //     (otherwise its component together with the (k+1)-core of G would already
 //     be a (k+1)-core of G).  Those vertices are found by a BFS, raised to
 //     min(core + 1, degree), and the h-index iteration settles them;
-//   * batches above a size threshold are applied in one rewrite and followed
-//     by a full decomposition, which is cheaper than many rounds.
+//   * batches above a size threshold (a larger one for batches of deletions
+//     only) are applied in one rewrite and followed by a full decomposition,
+//     which is cheaper than many rounds.
 #include <algorithm>
 #include <chrono>
 #include <cstring>
@@ -561,7 +562,11 @@ int graph_update(Graph *g, const uint32_t *ins_src, const uint32_t *ins_dst, uin
     if (!g->core_valid) KC_TRY(peel_run(g, s, false, nullptr));
     Scratch sc;
     sc.stream = s;
-    const bool incremental = n_ins + n_del <= (uint64_t)g->tune.update_incremental_max;
+    // deletions alone need no matching rounds: the h-index iteration from the
+    // old cores beats a full decomposition up to a few hundred thousand edges
+    // (R-MAT 22: 10^3 2.0 vs 8.4 ms, 10^5 6.3 vs 8.9 ms, 10^6 11.2 vs 10.6 ms)
+    const bool incremental = n_ins + n_del <= (uint64_t)g->tune.update_incremental_max ||
+                             (n_ins == 0 && n_del <= (uint64_t)g->tune.update_deletion_incremental_max);
     uint32_t *d_del_s = nullptr, *d_del_d = nullptr;
     if (n_del) {
         KC_TRY(sc.get(&d_del_s, n_del, "deleted edges"));

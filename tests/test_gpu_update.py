@@ -40,6 +40,7 @@ def test_update_batches_exact(incremental_max):
     rng = np.random.default_rng(12)
     g = pg.rmat_graph(14, 8, seed=21)
     g.set_param("update.incremental_max", incremental_max)
+    g.set_param("update.deletion_incremental_max", incremental_max)
     n = g.n
     g.decompose("peelone_dyn")
     for step, (ni, nd) in enumerate([(0, 300), (300, 0), (500, 500), (2000, 1500), (1, 1), (0, 0), (40, 4000)]):
@@ -165,4 +166,70 @@ def test_c5_rmat22_update_batches_exact(mode):
         bad = np.flatnonzero(core != want)
         assert bad.size == 0, (step, int(size), bad.size, st)
         keys = new_keys
+    g.free()
+
+
+def test_incremental_deletions_below_old_core():
+    """A deletion batch can leave a vertex with fewer edges than its old core
+    number, the upper bound the incremental path starts from: two vertices of
+    a 700-clique (core 699) keep 49 and 19 of their edges, so their rows take
+    the short-row paths of the h-index with estimates far above the row
+    length.  Also 30% of an R-MAT graph's edges deleted in one incremental
+    batch.  Both exact against Batagelj-Zaversnik on the updated graph."""
+    k = 700
+    a, b = np.triu_indices(k, 1)
+    g = pg.Graph.from_edges(a.astype(np.uint32), b.astype(np.uint32), k, dedup=True)
+    g.decompose("peelone_dyn")
+    g.set_param("update.incremental_max", 1 << 30)
+    ds = np.concatenate([np.zeros(650), np.ones(680)]).astype(np.uint32)
+    dd = np.concatenate([np.arange(50, 700), np.arange(20, 700)]).astype(np.uint32)
+    core, st = g.update(dels=(ds, dd))
+    assert st["recomputed"] == 0
+    rp, col = g.csr()
+    assert rp[1] - rp[0] == 49 and rp[2] - rp[1] == 19
+    want, _ = oracle.bz(rp, col)
+    assert np.array_equal(core, want)
+    g.free()
+
+    g = pg.rmat_graph(14, 16, seed=21)
+    rp, col = g.csr()
+    src = np.repeat(np.arange(g.n, dtype=np.uint32), np.diff(rp))
+    upper = src < col
+    es, ed = src[upper], col[upper]
+    pick = np.random.default_rng(5).choice(es.size, size=int(0.3 * es.size), replace=False)
+    g.decompose("peelone_dyn")
+    g.set_param("update.incremental_max", 1 << 30)
+    core, st = g.update(dels=(es[pick], ed[pick]))
+    assert st["recomputed"] == 0
+    rp, col = g.csr()
+    want, _ = oracle.bz(rp, col)
+    assert np.array_equal(core, want)
+    g.free()
+
+
+def test_deletion_batches_incremental_by_default():
+    """Batches of deletions only take the incremental path up to
+    update.deletion_incremental_max edges (default 500,000), mixed batches
+    only up to update.incremental_max (512); both exact."""
+    rng = np.random.default_rng(8)
+    g = pg.rmat_graph(15, 16, seed=4)
+    g.decompose("peelone_dyn")
+    rp, col = g.csr()
+    keys = edge_keys(rp, col)
+    ins, dels = random_batch(rng, keys, g.n, 0, 20000)
+    core, st = g.update(ins, dels)
+    assert st["recomputed"] == 0 and st["deleted"] == 20000
+    rp, col = g.csr()
+    assert np.array_equal(core, oracle.bz(rp, col)[0])
+    keys = edge_keys(rp, col)
+    ins, dels = random_batch(rng, keys, g.n, 1000, 1000)
+    core, st = g.update(ins, dels)
+    assert st["recomputed"] == 1
+    rp, col = g.csr()
+    assert np.array_equal(core, oracle.bz(rp, col)[0])
+    g.set_param("update.deletion_incremental_max", 100)
+    keys = edge_keys(rp, col)
+    ins, dels = random_batch(rng, keys, g.n, 0, 1000)
+    core, st = g.update(ins, dels)
+    assert st["recomputed"] == 1
     g.free()
