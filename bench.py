@@ -368,6 +368,8 @@ def run_engine(args, wl, world, rank, local, dist):
     for c in h_cores:
         free_cores.put(c)
 
+    phases = []  # (upload ms, decomposition ms) of each step, from the graph's CUDA events
+
     def e2e_step(_i=0):
         # one step through the public C ABI: pinned host CSR -> device graph,
         # decomposition with the core array written to pinned host memory
@@ -376,7 +378,10 @@ def run_engine(args, wl, world, rank, local, dist):
             h = pg.Graph.from_csr_ptr(h_rp.value, h_col.value, n, device=device)
             for name, val in args.param:
                 h.set_param(name, val)
-            pg.check(pg.lib().kc_decompose(h.handle, mid, pg.ctypes.c_void_p(out.value), 0, None, None))
+            est = pg.kc_stats()
+            pg.check(pg.lib().kc_decompose(h.handle, mid, pg.ctypes.c_void_p(out.value), 0, pg.ctypes.byref(est),
+                                           None))
+            phases.append((est.build_ms, est.ms))
             h.free()
         finally:
             free_cores.put(out)
@@ -392,19 +397,32 @@ def run_engine(args, wl, world, rank, local, dist):
         return allmax(dist, t1 - t0)
 
     e2e_step()
+    phases.clear()
     serial_s = timed(lambda: [e2e_step() for _ in range(e2e_steps)])
+    serial_up_ms = statistics.median(p[0] for p in phases) if phases else 0.0
     # the same steps from `depth` host threads: graph handles are independent,
     # so one step's upload overlaps the previous step's decomposition
     with ThreadPoolExecutor(depth) as ex:
         list(ex.map(e2e_step, range(depth)))
+        phases.clear()
         e2e_s = timed(lambda: list(ex.map(e2e_step, range(e2e_steps))))
+    up_ms = statistics.median(p[0] for p in phases) if phases else 0.0
+    dec_ms = statistics.median(p[1] for p in phases) if phases else 0.0
     _ = int(core_view[:n].max()) if n else 0
     line["e2e"] = {"value": round(m * e2e_steps * world / e2e_s / 1e6, 3), "unit": "M edges/s",
                    "h2d_bytes_per_step": 8 * (n + 1) + 4 * nnz, "d2h_bytes_per_step": 4 * n,
                    "steps": e2e_steps, "ms_per_step": round(1e3 * e2e_s / e2e_steps, 3),
                    "host_threads": depth,
                    "serial_value": round(m * e2e_steps * world / serial_s / 1e6, 3),
-                   "serial_ms_per_step": round(1e3 * serial_s / e2e_steps, 3)}
+                   "serial_ms_per_step": round(1e3 * serial_s / e2e_steps, 3),
+                   # per step, median: the upload's own time and rate (the
+                   # link runs at about 211 GB/s host to device), and the
+                   # decomposition's device time
+                   "upload_ms": round(up_ms, 3),
+                   "upload_GB_per_s": round((8 * (n + 1) + 4 * nnz) / (up_ms * 1e6), 1) if up_ms else None,
+                   "decompose_ms": round(dec_ms, 3),
+                   "serial_upload_GB_per_s": round((8 * (n + 1) + 4 * nnz) / (serial_up_ms * 1e6), 1)
+                   if serial_up_ms else None}
     for p in h_cores[1:]:
         pg.lib().kc_host_free(p)
     for p in (h_rp, h_col, h_core):
