@@ -90,6 +90,18 @@ def test_update_rejects_bad_ids_and_multigraphs():
     with pytest.raises(pg.KCoreError) as e:
         g.update(([0], [7]), None)
     assert e.value.code == pg.KC_ERR_INVALID
+    # the full path (ids checked on the device) rejects them too and leaves
+    # the graph as it was
+    g.set_param("update.incremental_max", 0)
+    g.set_param("update.deletion_incremental_max", 0)
+    for ins, dels in ((([0], [7]), None), (None, ([0], [9])), (([0], [2]), ([5], [1]))):
+        with pytest.raises(pg.KCoreError) as e:
+            g.update(ins, dels)
+        assert e.value.code == pg.KC_ERR_INVALID
+    rp, col = g.csr()
+    assert list(rp) == [0, 1, 3, 4] and list(col) == [1, 0, 2, 1]
+    core, st = g.update(([0], [2]), None)
+    assert list(core) == [2, 2, 2] and st["recomputed"] == 1
     h = pg.Graph.from_edges([0, 0, 1], [1, 1, 2], 3)  # parallel edge kept
     with pytest.raises(pg.KCoreError) as e:
         h.update(([0], [2]), None)
