@@ -15,8 +15,11 @@ Printed JSON line (rank 0):
              copies the CSR host->device (pinned), decomposes, copies the core
              array back and frees the graph; steps run from two host threads
              (independent graph handles), so one step's upload overlaps the
-             previous step's decomposition (serial_value: one thread); the
-             same K steps as value, the pipeline's fill (the first upload,
+             previous steps' decompositions (serial_value: one thread); its
+             graphs run the peel on one CTA per SM, so that two decompositions
+             share the GPU (a peel alone is latency-bound: 28.0 ms on half the
+             CTAs against 22.7 ms on all, but two at once take 17.8 ms each);
+             the same K steps as value, the pipeline's fill (the first upload,
              which overlaps nothing) inside the timed region;
   roofline   algorithmic bytes B = 10*nnz + 16*n + 8 per decomposition over the
              main kernel's average CUDA-event duration, against the measured
@@ -376,6 +379,8 @@ def run_engine(args, wl, world, rank, local, dist):
         out = free_cores.get()
         try:
             h = pg.Graph.from_csr_ptr(h_rp.value, h_col.value, n, device=device)
+            if args.e2e_ctas_per_sm:
+                h.set_param("peel.ctas_per_sm", args.e2e_ctas_per_sm)
             for name, val in args.param:
                 h.set_param(name, val)
             est = pg.kc_stats()
@@ -412,11 +417,14 @@ def run_engine(args, wl, world, rank, local, dist):
     line["e2e"] = {"value": round(m * e2e_steps * world / e2e_s / 1e6, 3), "unit": "M edges/s",
                    "h2d_bytes_per_step": 8 * (n + 1) + 4 * nnz, "d2h_bytes_per_step": 4 * n,
                    "steps": e2e_steps, "ms_per_step": round(1e3 * e2e_s / e2e_steps, 3),
-                   "host_threads": depth,
+                   "host_threads": depth, "peel_ctas_per_sm": args.e2e_ctas_per_sm or None,
                    "serial_value": round(m * e2e_steps * world / serial_s / 1e6, 3),
                    "serial_ms_per_step": round(1e3 * serial_s / e2e_steps, 3),
-                   # per step, median: the upload's own time and rate (the
-                   # link runs at about 211 GB/s host to device), and the
+                   # per step, median: the upload's time and rate from its
+                   # own CUDA events (with several steps in flight this
+                   # includes waiting for the copy engine behind another
+                   # step's upload; serial_upload_GB_per_s is the link's own
+                   # rate, about 211 GB/s host to device) and the
                    # decomposition's device time
                    "upload_ms": round(up_ms, 3),
                    "upload_GB_per_s": round((8 * (n + 1) + 4 * nnz) / (up_ms * 1e6), 1) if up_ms else None,
@@ -892,8 +900,10 @@ def main():
     ap.add_argument("--no-inputs", action="store_true", help="skip the input/output path section")
     ap.add_argument("--no-c2", action="store_true", help="skip the R-MAT scale 22 section")
     ap.add_argument("--no-refgpu", action="store_true", help="skip the reference GPU driver section")
-    ap.add_argument("--e2e-depth", type=int, default=2,
+    ap.add_argument("--e2e-depth", type=int, default=3,
                     help="end-to-end steps in flight (host threads with their own graph handles)")
+    ap.add_argument("--e2e-ctas-per-sm", type=int, default=1,
+                    help="peel.ctas_per_sm of the end-to-end graphs (0: the library's default, all resident CTAs)")
     ap.add_argument("--refgpu-graphs", default="er65536,rmat22",
                     help="graphs of the reference GPU driver section (er65536, rmat22)")
     ap.add_argument("--batch-graphs", type=int, default=4096, help="graphs in the batched section")
