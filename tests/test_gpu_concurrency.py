@@ -78,3 +78,31 @@ def test_updates_and_decompositions_in_parallel_threads():
     core, _ = big.decompose("peelone_dyn")
     assert np.array_equal(core, oracle.bz(rp, col)[0])
     big.free()
+
+
+def test_half_grid_peels_run_side_by_side():
+    """With peel.ctas_per_sm = 1 two cooperative peels fit on the GPU at once
+    (the end-to-end pipeline runs its graphs this way); three threads each
+    decompose their own graphs repeatedly, every result exact."""
+    cases = [_case(10 + i) for i in range(3)]
+    big = pg.rmat_graph(16, 16, seed=3)
+    rp_b, col_b = big.csr()
+    ref_b = oracle.bz(rp_b, col_b)[0]
+    big.free()
+
+    def work(i):
+        rp, col, ref = (rp_b, col_b, ref_b) if i % 2 == 0 else cases[i % 3]
+        g = pg.Graph.from_csr(rp, col)
+        try:
+            g.set_param("peel.ctas_per_sm", 1)
+            ok = True
+            for _ in range(4):
+                core, _ = g.decompose("peelone_dyn")
+                ok &= bool(np.array_equal(core, ref))
+            return ok
+        finally:
+            g.free()
+
+    with ThreadPoolExecutor(3) as ex:
+        results = list(ex.map(work, range(9)))
+    assert all(results)
