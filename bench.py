@@ -13,12 +13,13 @@ Printed JSON line (rank 0):
              (CUDA events on the launching stream), inputs resident in HBM;
   e2e        the same metric through the C ABI with host buffers: each step
              copies the CSR host->device (pinned), decomposes, copies the core
-             array back and frees the graph; steps run from two host threads
+             array back and frees the graph; steps run from three host threads
              (independent graph handles), so one step's upload overlaps the
-             previous steps' decompositions (serial_value: one thread); its
-             graphs run the peel on one CTA per SM, so that two decompositions
-             share the GPU (a peel alone is latency-bound: 28.0 ms on half the
-             CTAs against 22.7 ms on all, but two at once take 17.8 ms each);
+             previous steps' decompositions, and these graphs run the peel on
+             one CTA per SM so that two decompositions share the GPU (a peel
+             alone is latency-bound: 28.0 ms on half the CTAs against 22.7 ms
+             on all, but two at once take 17.8 ms each); serial_value: one
+             thread and the default grid;
              the same K steps as value, the pipeline's fill (the first upload,
              which overlaps nothing) inside the timed region;
   roofline   algorithmic bytes B = 10*nnz + 16*n + 8 per decomposition over the
@@ -373,13 +374,14 @@ def run_engine(args, wl, world, rank, local, dist):
 
     phases = []  # (upload ms, decomposition ms) of each step, from the graph's CUDA events
 
-    def e2e_step(_i=0):
+    def e2e_step(_i=0, shared=True):
         # one step through the public C ABI: pinned host CSR -> device graph,
-        # decomposition with the core array written to pinned host memory
+        # decomposition with the core array written to pinned host memory;
+        # `shared`: the GPU runs other steps' decompositions beside this one
         out = free_cores.get()
         try:
             h = pg.Graph.from_csr_ptr(h_rp.value, h_col.value, n, device=device)
-            if args.e2e_ctas_per_sm:
+            if shared and args.e2e_ctas_per_sm:
                 h.set_param("peel.ctas_per_sm", args.e2e_ctas_per_sm)
             for name, val in args.param:
                 h.set_param(name, val)
@@ -401,9 +403,9 @@ def run_engine(args, wl, world, rank, local, dist):
         barrier(dist)
         return allmax(dist, t1 - t0)
 
-    e2e_step()
+    e2e_step(shared=False)
     phases.clear()
-    serial_s = timed(lambda: [e2e_step() for _ in range(e2e_steps)])
+    serial_s = timed(lambda: [e2e_step(shared=False) for _ in range(e2e_steps)])
     serial_up_ms = statistics.median(p[0] for p in phases) if phases else 0.0
     # the same steps from `depth` host threads: graph handles are independent,
     # so one step's upload overlaps the previous step's decomposition
