@@ -399,9 +399,10 @@ int kc_server_free(kc_server *s);
  * rowptr[n] <= 4,194,304 entries; larger graphs get KC_ERR_CAPACITY.  The
  * only scratch is a fixed array of about 663 KB inside the library that every
  * GPU loading it holds until exit; it is looked up on the first call on each
- * device (make that first call before any stream capture).  All calls share
- * it: calls that overlap on the GPU race and must be serialised by the caller.
- * Nothing is allocated.  Blocks until the result is in core. */
+ * device.  All calls share it: calls that overlap on the GPU race and must be
+ * serialised by the caller.  Nothing is allocated.  Blocks until the result
+ * is in core (it reads a status word back and synchronises the stream), so a
+ * call can never be captured into a CUDA graph. */
 int kc_decompose_noalloc(const int64_t *d_rowptr, const uint32_t *d_col, uint32_t n, uint32_t *d_core,
                          void *stream);
 
