@@ -343,9 +343,11 @@ def run_engine(args, wl, world, rank, local, dist):
                      "kernel": kernel_name, "bytes_per_launch": bytes_alg,
                      "kernel_ms_avg": round(kavg, 4)},
         # kernels per decomposition: peel_ctl_reset + peel_init + peel_kernel
-        # (+ gpp_zero_to_one for gppeel); hindex_init + hindex_kernel
+        # (+ gpp_zero_to_one for gppeel); hindex_init + hx_order_rows (the
+        # degree-ordered copy of the long rows, unless hindex.order is 0) +
+        # hindex_kernel
         "gpu_launches": args.steps * ((4 if pg.method_id(method) == 4 else 3) if kernel_name == "peel_kernel"
-                                      else 2),
+                                      else (2 if dict(args.param).get("hindex.order", 1) == 0 else 3)),
         "clocks": sampler.summary(t_load0, t_load1),
     }
 

