@@ -359,9 +359,9 @@ static int from_csr_common(const int64_t *rowptr, const uint32_t *col, uint32_t 
     release_event(a);
     release_event(b);
     if (e != cudaSuccess) { delete g; return fail(KC_ERR_CUDA, "CSR upload: %s", cudaGetErrorString(e)); }
-    // degree statistics on the device (one pass over rowptr in HBM): host
-    // threads scanning a host CSR while it uploads were measured to stretch
-    // steps by up to 20 ms on hosts busy with other work
+    // degree statistics on the device: one pass over rowptr in HBM (about
+    // 0.1 ms for 33.5 M rows) instead of host threads scanning the host CSR,
+    // which compete with whatever else the host runs
     rc = graph_finish(g);
     if (rc) { delete g; return rc; }
     if (g->max_deg >= 0x7fffffffu) { delete g; return fail(KC_ERR_UNSUPPORTED, "degree above 2^31-1"); }
