@@ -409,6 +409,7 @@ def run_engine(args, wl, world, rank, local, dist):
     phases.clear()
     serial_s = timed(lambda: [e2e_step(shared=False) for _ in range(e2e_steps)])
     serial_up_ms = statistics.median(p[0] for p in phases) if phases else 0.0
+    serial_dec_ms = statistics.median(p[1] for p in phases) if phases else 0.0
     # the same steps from `depth` host threads: graph handles are independent,
     # so one step's upload overlaps the previous step's decomposition
     with ThreadPoolExecutor(depth) as ex:
@@ -434,7 +435,11 @@ def run_engine(args, wl, world, rank, local, dist):
                    "upload_GB_per_s": round((8 * (n + 1) + 4 * nnz) / (up_ms * 1e6), 1) if up_ms else None,
                    "decompose_ms": round(dec_ms, 3),
                    "serial_upload_GB_per_s": round((8 * (n + 1) + 4 * nnz) / (serial_up_ms * 1e6), 1)
-                   if serial_up_ms else None}
+                   if serial_up_ms else None,
+                   # one thread: a step's wall time = upload + decomposition +
+                   # the rest (graph set-up and free, host calls, the read-back)
+                   "serial_decompose_ms": round(serial_dec_ms, 3),
+                   "serial_other_ms": round(1e3 * serial_s / e2e_steps - serial_up_ms - serial_dec_ms, 3)}
     for p in h_cores[1:]:
         pg.lib().kc_host_free(p)
     for p in (h_rp, h_col, h_core):
