@@ -60,3 +60,24 @@ def test_serving_exactness_replay_detects_a_wrong_result():
     assert bench.serve_exact(rp, col, reqs, res) == (True, 4)
     res[1]["digest"] += 1
     assert bench.serve_exact(rp, col, reqs, res) == (False, 4)
+
+
+def test_param_option_and_e2e_defaults():
+    """--param NAME=VALUE (decimal or 0x) reaches the tunables of the main
+    graph; the end-to-end section defaults to three steps in flight with the
+    peel on one CTA per SM."""
+    import argparse
+
+    import pytest
+    sys.path.insert(0, ROOT)
+    import bench
+    assert bench._param("hindex.order=0") == ("hindex.order", 0)
+    assert bench._param("peel.chunk=0x800") == ("peel.chunk", 2048)
+    for bad in ("hindex.order", "=3", "x=y"):
+        with pytest.raises((argparse.ArgumentTypeError, ValueError)):
+            bench._param(bad)
+    out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--help"], capture_output=True, text=True,
+                         timeout=120, cwd=ROOT)
+    assert out.returncode == 0 and "--param NAME=VALUE" in out.stdout
+    src = open(os.path.join(ROOT, "bench.py")).read()
+    assert '"--e2e-depth", type=int, default=3' in src and '"--e2e-ctas-per-sm", type=int, default=1' in src
