@@ -36,3 +36,36 @@ def test_cli_drivers_built():
         p = os.path.join(pb.BIN, name)
         if os.path.exists(os.path.join(pb.CLI, name + ".cpp")):
             assert os.access(p, os.X_OK), p
+
+
+def test_header_compiles_as_c99_and_cxx(tmp_path):
+    """include/kcore.h is a plain C header (the boundary a cgo / JNI / ctypes
+    host binds): it compiles on its own as C99 and as C++17, and a C++
+    program that includes it links against libkcore.so and runs."""
+    import shutil
+    import subprocess
+    from pico_gb300 import build as pb
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    inc = os.path.join(root, "include")
+    c = tmp_path / "use.c"
+    c.write_text('#include "kcore.h"\nint f(kc_graph *g) { kc_stats st; return kc_decompose(g, KC_PEELONE_DYN, '
+                 '0, 0, &st, 0) + (int)st.kmax + KC_ABI_VERSION; }\n')
+    for cc, std, src in (("gcc", "-std=c99", c), ("g++", "-std=c++17", c)):
+        if shutil.which(cc) is None:
+            continue
+        args = [cc, std, "-Wall", "-Werror", "-fsyntax-only", "-I", inc]
+        if cc == "g++":
+            args += ["-x", "c++"]
+        r = subprocess.run(args + [str(src)], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+    lib = pb.LIB
+    if shutil.which("g++") and os.path.exists(lib):
+        cpp = tmp_path / "app.cpp"
+        cpp.write_text('#include "kcore.h"\n#include <cstdio>\nint main() { std::printf("%d\\n", kc_abi_version()); '
+                       'return 0; }\n')
+        exe = tmp_path / "app"
+        r = subprocess.run(["g++", "-I", inc, str(cpp), "-L", os.path.dirname(lib), "-lkcore",
+                            "-Wl,-rpath," + os.path.dirname(lib), "-o", str(exe)], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+        r = subprocess.run([str(exe)], capture_output=True, text=True)
+        assert r.returncode == 0 and r.stdout.strip() == "1", (r.stdout, r.stderr)
